@@ -1,0 +1,232 @@
+/*
+ * visg_sim.h — C ABI of the GB300-native VISGSim cloth step.
+ *
+ * Drop-in boundary for the reference's `Simulator` class (src/simulator.h:9-59):
+ * plain C types, pointers and sizes only; every call returns an int status
+ * (VISG_OK = 0, negative on error) and never throws.  One handle owns all of its
+ * device memory; calls on one handle are not thread-safe; calls on different
+ * handles are independent.  Work is issued on the handle's CUDA stream
+ * (visg_set_stream; the legacy default stream unless set) and is asynchronous
+ * unless the function says it synchronises.
+ *
+ * Physics follows src/verlet.cu:24-161 (fused Verlet step, damped CSR springs,
+ * inelastic force projection and first-hit BVH position projection) and the LBVH
+ * of src/bvh/{bvh.cu,cudaBRT.cu,primitive.cu,bbox.h}.  Where the reference is
+ * undefined or buggy the behaviour chosen here is stated next to the call.
+ */
+#ifndef VISG_SIM_H
+#define VISG_SIM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define VISG_OK               0
+#define VISG_ERR_INVALID_ARG (-1) /* bad size, null pointer, index out of range      */
+#define VISG_ERR_CUDA        (-2) /* a CUDA runtime call failed; see visg_last_error */
+#define VISG_ERR_OOM         (-3) /* device allocation failed                        */
+#define VISG_ERR_NO_DEVICE   (-4) /* no CUDA device visible                          */
+#define VISG_ERR_DIVERGED    (-5) /* NaN/Inf or displacement above the limit seen    */
+#define VISG_ERR_TIMEOUT     (-6) /* a bounded device-side wait gave up              */
+#define VISG_ERR_STATE       (-7) /* call not valid in the handle's current state    */
+#define VISG_ERR_UNSUPPORTED (-8) /* input the chosen path cannot handle             */
+
+#define VISG_MAX_LISTS 4
+
+/* One directed CSR spring entry.  Same layout as the reference's s_spring
+ * (src/spring.h:8-12): `end` is the other vertex, `rest` the rest length. */
+typedef struct VisgSpring {
+    int32_t end;
+    float rest;
+} VisgSpring;
+
+/* Physics and pipeline parameters.  visg_default_params() fills the reference's
+ * constants (src/verlet.cu:12-21,62; src/simulation.cu:132; src/bvh/primitive.cu:21). */
+typedef struct VisgParams {
+    float dt;              /* time step                              (verlet.cu:17, 1/40)      */
+    float mass;            /* per-vertex mass                        (verlet.cu:16, 0.3)       */
+    float gravity[3];      /* acceleration                           (verlet.cu:19-21)         */
+    float force_damping;   /* F += force_damping * v                 (verlet.cu:15, -0.02)     */
+    float spring_damping;  /* kd of every spring                     (verlet.cu:62, -0.5)      */
+    float verlet_damping;  /* gamma: x' = x + gamma*(x - x_old) + a dt^2.  Exactly 1.0 selects
+                              the reference expression 2x - x_old + a dt^2 (verlet.cu:155).      */
+    float thickness;       /* body vertices pushed along their normal once per body upload
+                              (Mesh::vertex_extend, Mesh.cpp:101-117; simulation.cu:132, 0.003) */
+    float box_depth;       /* expanded triangle box depth            (primitive.cu:21, 0.01)   */
+    int32_t n_lists;       /* number of spring lists, 1..VISG_MAX_LISTS (reference: 2)         */
+    float list_k[VISG_MAX_LISTS]; /* stiffness of each list          (verlet.cu:13-14, 100, 2) */
+    int32_t collide;       /* 1: body collision on (reference), 0: off                          */
+    int32_t check_every;   /* every K steps check for NaN/Inf and |dx| > max_displacement; 0=off */
+    float max_displacement;/* limit for the divergence check (metres per step)                  */
+    int32_t use_graph;     /* 1: replay multi-step loops as CUDA graphs (default), 0: launches  */
+} VisgParams;
+
+void visg_default_params(VisgParams* p);
+
+/* Library / device information.  Returns a static string; never NULL. */
+const char* visg_version(void);
+/* Message of the last failing call on this thread (any handle); never NULL. */
+const char* visg_last_error(void);
+
+/* ======================================================================== */
+/* Plain form: one garment, one body.                                         */
+/* ======================================================================== */
+typedef struct VisgSim VisgSim;
+
+/* Replaces Simulator(Mesh& cloth, Mesh& body) (src/simulation.cu:47-100,102-125,127-138).
+ *   cloth_xyz   n_vertices*3 floats; initial x and x_old (zero velocity, simulation.cu:84-85)
+ *   csr_row[l]  n_vertices+1 row offsets of spring list l (CSR_R_*, simulator.h:45-46)
+ *   csr[l]      csr_row[l][n_vertices] entries of list l (CSR_C_*), entries of one row in
+ *               the order the forces are summed
+ *   list_k      NULL, or per list NULL / one stiffness per entry of that list (overrides
+ *               params->list_k[l] entry by entry; needed for per-spring gradients)
+ *   body_xyz    n_body_vertices*3 floats, body_normals NULL or n_body_vertices*3 floats;
+ *               with normals the vertices are pushed by params->thickness along them
+ *   tris        n_tris*3 vertex indices.  n_tris == 0 disables collision.
+ * The LBVH is built before the call returns (asynchronously on the stream). */
+int visg_create(const VisgParams* params,
+                const float* cloth_xyz, int32_t n_vertices,
+                const uint32_t* const* csr_row, const VisgSpring* const* csr,
+                const float* const* list_k,
+                const float* body_xyz, const float* body_normals, int32_t n_body_vertices,
+                const uint32_t* tris, int32_t n_tris,
+                VisgSim** out);
+
+/* Frees everything (~Simulator, simulation.cu:28-45). Synchronises the stream. */
+int visg_destroy(VisgSim* sim);
+
+/* Launch subsequent work on `cuda_stream` (a cudaStream_t; NULL = legacy default). */
+int visg_set_stream(VisgSim* sim, void* cuda_stream);
+
+/* Replaces Simulator::simulate (simulation.cu:141-150) without the GL update:
+ * `nsteps` fused steps, ping-ponging the state buffers (swap_buffer, :243-251). */
+int visg_step(VisgSim* sim, int32_t nsteps);
+
+/* New (the reference has no moving body): upload new body vertex positions (and
+ * normals, for the thickness push) and rebuild the LBVH on the device:
+ * expanded boxes -> root box -> Morton codes -> radix sort -> de-duplication ->
+ * radix-tree build and refit (bvh.cu:154-297, cudaBRT.cu:120-206). */
+int visg_update_body(VisgSim* sim, const float* body_xyz, const float* body_normals);
+
+/* Same with the vertices already in device memory (n_body_vertices*3 floats). */
+int visg_update_body_device(VisgSim* sim, const float* d_body_xyz, const float* d_body_normals);
+
+/* Replaces Simulator::update_vertex (simulation.cu:253-257): sets x and x_old of
+ * one vertex (its velocity becomes zero). */
+int visg_set_vertex(VisgSim* sim, uint32_t idx, const float xyz[3]);
+
+/* Pinned vertices keep x and get x_old = x every step (the reference's drag via
+ * update_vertex called before every step). n == 0 clears all pins. */
+int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n);
+
+/* Headless replacement of cuda_update_vbo's position upload (simulation.cu:196-216):
+ * writes n_vertices*3 floats of the current positions.  on_device = 1: `out` is a
+ * device pointer and the copy is asynchronous; 0: host pointer (pinned or pageable),
+ * synchronises and reports any device-side error (divergence, timeout). */
+int visg_get_positions(VisgSim* sim, float* out, int32_t on_device);
+
+/* Full step state (x, x_old, previous contact normal; n_vertices*3 floats each, host).
+ * Any pointer may be NULL.  get synchronises. */
+int visg_get_state(VisgSim* sim, float* x, float* x_old, float* normal);
+int visg_set_state(VisgSim* sim, const float* x, const float* x_old, const float* normal);
+
+/* Waits for the stream; returns the first device-side error recorded since the
+ * last call (VISG_ERR_DIVERGED, VISG_ERR_TIMEOUT) or VISG_OK. */
+int visg_sync(VisgSim* sim);
+
+int visg_get_info(VisgSim* sim, int32_t* n_vertices, int32_t* n_entries,
+                  int32_t* n_tris, int32_t* n_leaves);
+
+/* Inspection of the current LBVH in the reference's layout (bvh.cu:264-297,
+ * cudaBRT.h:34-115).  Arrays are host memory sized for n_tris (per-triangle) or
+ * n_leaves = T' (after de-duplication); any pointer may be NULL.
+ *   tri_codes[T], tri_boxes[T*6] (min xyz, max xyz) — per input triangle
+ *   sorted_codes[T'], sorted_tris[T']
+ *   child_a/child_b/parent_internal[T'-1], parent_leaf[T'] — encoded as in
+ *       BRTreeNode: +(i+1) internal, -(i+1) leaf, 0 none; root is internal 0
+ *   internal_boxes[(T'-1)*6], leaf_boxes[T'*6], root_box[6] (the Morton frame)
+ * Synchronises. */
+int visg_export_lbvh(VisgSim* sim, uint32_t* tri_codes, float* tri_boxes,
+                     uint32_t* sorted_codes, int32_t* sorted_tris,
+                     int32_t* child_a, int32_t* child_b,
+                     int32_t* parent_internal, int32_t* parent_leaf,
+                     float* internal_boxes, float* leaf_boxes, float* root_box);
+
+/* First-hit query of the current LBVH (D_BVH::intersect + primitive_intersect,
+ * cudaBRT.cu:239-289, primitive.cu:110-125) for n host points: leaf[i] = the leaf
+ * index (sorted order) or -1, inside[i] = plane test, dist[i], normal[i*3].
+ * Any output may be NULL.  Synchronises. */
+int visg_query_points(VisgSim* sim, const float* points, int32_t n,
+                      int32_t* leaf, int32_t* inside, float* dist, float* normal);
+
+/* ---- differentiation (hand-written adjoint) ---------------------------------
+ * visg_forward runs `nsteps` steps recording a checkpoint of (x, x_old, normal)
+ * every `checkpoint_every` steps; the contact set of each step is frozen as the
+ * forward pass found it.  visg_backward then propagates dL/dx_final (and optional
+ * dL/dx_old_final), n_vertices*3 host floats, back through those steps,
+ * recomputing the steps between checkpoints, and writes
+ *   dL_dk[e]     per CSR entry, lists concatenated in order (host, total entries)
+ *   dL_dscalar[3] = dL/d verlet_damping, dL/d force_damping, dL/d spring_damping.
+ * Requires a symmetric spring graph (every i->j entry has a j->i entry in the
+ * same list); VISG_ERR_UNSUPPORTED otherwise.  Body is held static. */
+int visg_forward(VisgSim* sim, int32_t nsteps, int32_t checkpoint_every);
+int visg_backward(VisgSim* sim, const float* dL_dx, const float* dL_dxold,
+                  float* dL_dk, float* dL_dscalar);
+
+/* ======================================================================== */
+/* Batched form: many garments, each with its own body, one launch per step.  */
+/* ======================================================================== */
+typedef struct VisgBatch VisgBatch;
+
+int visg_batch_create(const VisgParams* params, VisgBatch** out);
+/* Adds one garment with its body; arguments as visg_create plus pins.  Returns the
+ * garment id in *garment.  Only valid before visg_batch_finalize. */
+int visg_batch_add(VisgBatch* b,
+                   const float* cloth_xyz, int32_t n_vertices,
+                   const uint32_t* const* csr_row, const VisgSpring* const* csr,
+                   const float* const* list_k,
+                   const uint32_t* pinned, int32_t n_pinned,
+                   const float* body_xyz, const float* body_normals, int32_t n_body_vertices,
+                   const uint32_t* tris, int32_t n_tris,
+                   int32_t* garment);
+/* Uploads all garments, builds every body's LBVH.  After this, step/query calls. */
+int visg_batch_finalize(VisgBatch* b);
+int visg_batch_set_stream(VisgBatch* b, void* cuda_stream);
+/* nsteps persistent launches (one per step) over all garments; with use_graph the
+ * loop is replayed from a captured CUDA graph. */
+int visg_batch_step(VisgBatch* b, int32_t nsteps);
+/* garment = -1: all garments concatenated in id order. */
+int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device);
+int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]);
+int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* body_xyz,
+                           const float* body_normals);
+/* Times the candidate launch shapes of the step kernel on this batch's own data
+ * and keeps the fastest; *block and *ctas_per_sm (may be NULL) report the choice.
+ * Leaves the simulation state unchanged. */
+int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm);
+int visg_batch_info(VisgBatch* b, int32_t* n_garments, int64_t* n_vertices,
+                    int64_t* n_entries, int64_t* n_tris);
+int visg_batch_sync(VisgBatch* b);
+int visg_batch_destroy(VisgBatch* b);
+
+/* ======================================================================== */
+/* Host-side scene helpers (no GPU needed).                                   */
+/* ======================================================================== */
+
+/* Reference spring topology from a triangle mesh (Springs::create_neigh +
+ * CSR_spring, src/spring.cpp:286-353,374-391): list 0 = structure springs (unique
+ * edge neighbours in face order), list 1 = bend springs (vertices opposite across
+ * each shared edge).  rest = initial distance.  Call with NULL outputs to get the
+ * entry counts, then again with arrays of n_vertices+1 rows and the counted entries. */
+int visg_springs_from_mesh(const float* xyz, int32_t n_vertices,
+                           const uint32_t* tris, int32_t n_tris,
+                           uint32_t* row0, VisgSpring* ent0, int32_t* n_ent0,
+                           uint32_t* row1, VisgSpring* ent1, int32_t* n_ent1);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VISG_SIM_H */

@@ -1,0 +1,1021 @@
+// visg_api.cu — the C ABI of include/visg_sim.h over one engine type.
+//
+// An Engine holds G >= 1 garments, each with its own body: the plain form
+// (VisgSim, the reference's Simulator, src/simulator.h:9-59) is an engine with one
+// garment; the batched form (VisgBatch) is the same engine with many.  All device
+// memory of an engine is one allocation carved by an Arena.  Steps are launched
+// on the user's stream; multi-step loops are replayed from CUDA graphs captured on
+// an internal stream (two graphs, one per ping-pong parity).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "visg_internal.cuh"
+
+using namespace visg;
+
+namespace {
+
+thread_local std::string g_err = "";
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? VISG_ERR_OOM : VISG_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CU(call)                                          \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+constexpr int kBlocks[3] = {128, 256, 512};
+int block_index(int b) { return b == 128 ? 0 : (b == 256 ? 1 : (b == 512 ? 2 : -1)); }
+
+struct GarmentIn {
+    std::vector<float> xyz;
+    int N = 0;
+    std::vector<std::vector<uint32_t>> rows;
+    std::vector<std::vector<VisgSpring>> ents;
+    std::vector<std::vector<float>> ks;
+    std::vector<uint32_t> pinned;
+    std::vector<float> bxyz, bnrm;
+    int nv = 0, nt = 0;
+    std::vector<uint32_t> tris;
+};
+
+int validate_params(const VisgParams* p) {
+    if (!p) return fail(VISG_ERR_INVALID_ARG, "params is NULL");
+    if (p->n_lists < 1 || p->n_lists > VISG_MAX_LISTS) return fail(VISG_ERR_INVALID_ARG, "n_lists must be 1..4");
+    if (!(p->dt > 0.0f) || !(p->mass > 0.0f)) return fail(VISG_ERR_INVALID_ARG, "dt and mass must be > 0");
+    return VISG_OK;
+}
+
+}  // namespace
+
+namespace visg {
+
+cudaError_t Arena::commit() {
+    size = 0;
+    for (auto& pl : plan) size += pl.second;
+    if (size == 0) size = 256;
+    cudaError_t e = cudaMalloc((void**)&base, size);
+    if (e != cudaSuccess) {
+        base = nullptr;
+        return e;
+    }
+    e = cudaMemset(base, 0, size);
+    if (e != cudaSuccess) return e;
+    used = 0;
+    for (auto& pl : plan) {
+        *pl.first = base + used;
+        used += pl.second;
+    }
+    plan.clear();
+    return cudaSuccess;
+}
+
+void Arena::release() {
+    if (base) cudaFree(base);
+    base = nullptr;
+    size = used = 0;
+}
+
+}  // namespace visg
+
+struct Engine {
+    VisgParams p{};
+    cudaStream_t stream = nullptr;
+    cudaStream_t cap = nullptr;
+    bool finalized = false;
+    std::vector<GarmentIn> gin;
+    int G = 0;
+    int64_t N = 0, E = 0;
+    std::vector<int64_t> voff, eoff;
+    std::vector<int64_t> merged_pos;  // merged entry -> index in (garment, list, entry) order
+    std::vector<uint32_t> h_rowp;
+    bool perk = false, any_body = false;
+    Arena arena;
+    float4* d_state[2] = {nullptr, nullptr};
+    float4* d_normal = nullptr;
+    uint32_t* d_rowp = nullptr;
+    uint2* d_ent = nullptr;
+    float* d_k = nullptr;
+    int4* d_tiles[3] = {nullptr, nullptr, nullptr};
+    int n_tiles[3] = {0, 0, 0};
+    BvhView* d_views = nullptr;
+    std::vector<BvhBuffers> bvh;
+    int* d_err = nullptr;
+    uint32_t* d_check = nullptr;
+    float* d_stage = nullptr;  // 9*N floats
+    uint32_t* h_status = nullptr;  // pinned: err, check0, check1
+    int cur = 0;
+    int block = 256, grid = 0;
+    int64_t steps_since_check = 0;
+    cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
+    int chunk_steps = 16;
+    std::vector<cudaGraphExec_t> body_exec;
+    int sm_count = 0;
+    // adjoint records
+    struct Adj {
+        int ckpt_every = 0, nsteps = 0;
+        std::vector<float4*> ck_state;  // checkpoints (2N float4 each)
+        std::vector<float4*> ck_normal;
+        float4* seg_state = nullptr;    // ckpt_every+1 states of the segment being replayed
+        float4* seg_hit = nullptr;      // ckpt_every hit records
+        float4* seg_nin = nullptr;      // ckpt_every normals entering each step
+        float4* lam[2] = {nullptr, nullptr};
+        float4* G = nullptr;
+        float* dk = nullptr;
+        double* dsc = nullptr;
+        uint32_t* rev = nullptr;
+        int start_cur = 0;
+        bool ready = false;
+    } adj;
+
+    ~Engine() {
+        if (stream) cudaStreamSynchronize(stream);
+        destroy_graphs();
+        free_adjoint();
+        arena.release();
+        if (h_status) cudaFreeHost(h_status);
+        if (cap) cudaStreamDestroy(cap);
+    }
+
+    void destroy_graphs() {
+        for (int c = 0; c < 2; ++c)
+            if (chunk_exec[c]) {
+                cudaGraphExecDestroy(chunk_exec[c]);
+                chunk_exec[c] = nullptr;
+            }
+        for (auto& g : body_exec)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    void free_adjoint() {
+        for (auto* q : adj.ck_state) cudaFree(q);
+        for (auto* q : adj.ck_normal) cudaFree(q);
+        adj.ck_state.clear();
+        adj.ck_normal.clear();
+        void* ps[] = {adj.seg_state, adj.seg_hit, adj.seg_nin, adj.lam[0], adj.lam[1], adj.G, adj.dk, adj.dsc, adj.rev};
+        for (void* q : ps)
+            if (q) cudaFree(q);
+        adj = Adj();
+    }
+
+    int add(const float* cloth, int n, const uint32_t* const* rows, const VisgSpring* const* csr,
+            const float* const* list_k, const uint32_t* pinned, int n_pinned, const float* body, const float* bn,
+            int nv, const uint32_t* tris, int nt, int* gid) {
+        if (finalized) return fail(VISG_ERR_STATE, "garments can only be added before finalize");
+        if (!cloth || n <= 0) return fail(VISG_ERR_INVALID_ARG, "cloth_xyz is NULL or n_vertices <= 0");
+        if (!rows || !csr) return fail(VISG_ERR_INVALID_ARG, "csr_row/csr is NULL");
+        if (nt < 0 || nv < 0 || (nt > 0 && (!body || !tris || nv <= 0)))
+            return fail(VISG_ERR_INVALID_ARG, "body arrays are NULL or sizes negative");
+        if (N + n > (int64_t)END_MASK) return fail(VISG_ERR_INVALID_ARG, "too many vertices");
+        GarmentIn g;
+        g.N = n;
+        g.xyz.assign(cloth, cloth + 3 * (size_t)n);
+        const int L = p.n_lists;
+        g.rows.resize(L);
+        g.ents.resize(L);
+        g.ks.resize(L);
+        for (int l = 0; l < L; ++l) {
+            if (!rows[l]) return fail(VISG_ERR_INVALID_ARG, "csr_row[l] is NULL");
+            g.rows[l].assign(rows[l], rows[l] + n + 1);
+            if (g.rows[l][0] != 0) return fail(VISG_ERR_INVALID_ARG, "csr_row[l][0] must be 0");
+            for (int i = 0; i < n; ++i)
+                if (g.rows[l][i + 1] < g.rows[l][i]) return fail(VISG_ERR_INVALID_ARG, "csr_row not monotonic");
+            uint32_t El = g.rows[l][n];
+            if (El > 0 && !csr[l]) return fail(VISG_ERR_INVALID_ARG, "csr[l] is NULL");
+            g.ents[l].assign(csr[l], csr[l] + El);
+            for (auto& e : g.ents[l])
+                if (e.end < 0 || e.end >= n) return fail(VISG_ERR_INVALID_ARG, "spring end out of range");
+            if (list_k && list_k[l]) g.ks[l].assign(list_k[l], list_k[l] + El);
+        }
+        for (int k = 0; k < n_pinned; ++k) {
+            if (pinned[k] >= (uint32_t)n) return fail(VISG_ERR_INVALID_ARG, "pinned index out of range");
+            g.pinned.push_back(pinned[k]);
+        }
+        g.nv = nv;
+        g.nt = nt;
+        if (nt > 0) {
+            g.bxyz.assign(body, body + 3 * (size_t)nv);
+            if (bn) g.bnrm.assign(bn, bn + 3 * (size_t)nv);
+            g.tris.assign(tris, tris + 3 * (size_t)nt);
+            for (uint32_t t : g.tris)
+                if (t >= (uint32_t)nv) return fail(VISG_ERR_INVALID_ARG, "triangle index out of range");
+        }
+        N += n;
+        gin.push_back(std::move(g));
+        if (gid) *gid = (int)gin.size() - 1;
+        return VISG_OK;
+    }
+
+    int finalize() {
+        if (finalized) return fail(VISG_ERR_STATE, "already finalized");
+        if (gin.empty()) return fail(VISG_ERR_INVALID_ARG, "no garments");
+        int dev = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+        CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        CU(cudaHostAlloc((void**)&h_status, 16, cudaHostAllocDefault));
+        G = (int)gin.size();
+        const int L = p.n_lists;
+        voff.assign(G + 1, 0);
+        eoff.assign(G + 1, 0);
+        for (int g = 0; g < G; ++g) {
+            voff[g + 1] = voff[g] + gin[g].N;
+            int64_t e = 0;
+            for (int l = 0; l < L; ++l) e += gin[g].rows[l][gin[g].N];
+            eoff[g + 1] = eoff[g] + e;
+            for (int l = 0; l < L; ++l)
+                if (!gin[g].ks[l].empty()) perk = true;
+            if (gin[g].nt > 0) any_body = true;
+        }
+        E = eoff[G];
+        if (E >= (int64_t)ROW_MASK) return fail(VISG_ERR_INVALID_ARG, "too many spring entries");
+        // merged CSR
+        h_rowp.assign(N + 1, 0);
+        std::vector<uint2> ent(E > 0 ? E : 1);
+        std::vector<float> kk;
+        if (perk) kk.resize(E);
+        merged_pos.resize(E);
+        int64_t c = 0;
+        for (int g = 0; g < G; ++g) {
+            const GarmentIn& gi = gin[g];
+            std::vector<int64_t> lbase(L, 0);
+            for (int l = 1; l < L; ++l) lbase[l] = lbase[l - 1] + gi.rows[l - 1][gi.N];
+            for (int i = 0; i < gi.N; ++i) {
+                h_rowp[voff[g] + i] = (uint32_t)c;
+                for (int l = 0; l < L; ++l) {
+                    for (uint32_t e = gi.rows[l][i]; e < gi.rows[l][i + 1]; ++e) {
+                        uint32_t j = (uint32_t)(voff[g] + gi.ents[l][e].end);
+                        uint32_t rest;
+                        std::memcpy(&rest, &gi.ents[l][e].rest, 4);
+                        ent[c] = make_uint2(j | ((uint32_t)l << LIST_SHIFT), rest);
+                        if (perk) kk[c] = gi.ks[l].empty() ? p.list_k[l] : gi.ks[l][e];
+                        merged_pos[c] = eoff[g] + lbase[l] + e;
+                        ++c;
+                    }
+                }
+            }
+            for (uint32_t v : gi.pinned) h_rowp[voff[g] + v] |= PIN_BIT;
+        }
+        h_rowp[N] = (uint32_t)E;
+        // tiles for each block size
+        std::vector<std::vector<int4>> tiles(3);
+        for (int b = 0; b < 3; ++b)
+            for (int g = 0; g < G; ++g)
+                for (int64_t v = voff[g]; v < voff[g + 1]; v += kBlocks[b])
+                    tiles[b].push_back(make_int4(g, (int)v, (int)std::min<int64_t>(v + kBlocks[b], voff[g + 1]), 0));
+        // plan the allocation
+        arena.want(&d_state[0], 2 * (size_t)N + 2);
+        arena.want(&d_state[1], 2 * (size_t)N + 2);
+        arena.want(&d_normal, (size_t)N + 1);
+        arena.want(&d_rowp, (size_t)N + 2);
+        arena.want(&d_ent, (size_t)E + 1);
+        if (perk) arena.want(&d_k, (size_t)E + 1);
+        for (int b = 0; b < 3; ++b) {
+            n_tiles[b] = (int)tiles[b].size();
+            arena.want(&d_tiles[b], tiles[b].size() + 1);
+        }
+        arena.want(&d_views, (size_t)G);
+        arena.want(&d_err, 4);
+        arena.want(&d_check, 4);
+        arena.want(&d_stage, 9 * (size_t)N + 4);
+        bvh.resize(G);
+        for (int g = 0; g < G; ++g)
+            if (gin[g].nt > 0) bvh[g].plan(arena, gin[g].nv, gin[g].nt, !gin[g].bnrm.empty());
+        CU(arena.commit());
+        // upload
+        std::vector<float4> st(2 * (size_t)N);
+        for (int g = 0; g < G; ++g)
+            for (int i = 0; i < gin[g].N; ++i) {
+                const float* q = &gin[g].xyz[3 * (size_t)i];
+                int64_t v = voff[g] + i;
+                st[2 * v] = make_float4(q[0], q[1], q[2], q[0]);
+                st[2 * v + 1] = make_float4(q[1], q[2], 0.0f, 0.0f);
+            }
+        CU(cudaMemcpy(d_state[0], st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_rowp, h_rowp.data(), h_rowp.size() * 4, cudaMemcpyHostToDevice));
+        if (E > 0) CU(cudaMemcpy(d_ent, ent.data(), E * sizeof(uint2), cudaMemcpyHostToDevice));
+        if (perk && E > 0) CU(cudaMemcpy(d_k, kk.data(), E * sizeof(float), cudaMemcpyHostToDevice));
+        for (int b = 0; b < 3; ++b)
+            CU(cudaMemcpy(d_tiles[b], tiles[b].data(), tiles[b].size() * sizeof(int4), cudaMemcpyHostToDevice));
+        std::vector<BvhView> views(G);
+        for (int g = 0; g < G; ++g)
+            views[g] = gin[g].nt > 0 ? bvh[g].view() : BvhView{nullptr, nullptr, nullptr};
+        CU(cudaMemcpy(d_views, views.data(), G * sizeof(BvhView), cudaMemcpyHostToDevice));
+        body_exec.assign(G, nullptr);
+        for (int g = 0; g < G; ++g) {
+            if (gin[g].nt == 0) continue;
+            CU(cudaMemcpy(bvh[g].xyz_in, gin[g].bxyz.data(), gin[g].bxyz.size() * 4, cudaMemcpyHostToDevice));
+            if (!gin[g].bnrm.empty())
+                CU(cudaMemcpy(bvh[g].nrm_in, gin[g].bnrm.data(), gin[g].bnrm.size() * 4, cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(bvh[g].tris, gin[g].tris.data(), gin[g].tris.size() * 4, cudaMemcpyHostToDevice));
+            CU(lbvh_build(bvh[g], p.thickness, p.box_depth, d_err, stream));
+        }
+        // keep only what later calls need
+        for (auto& g : gin) {
+            std::vector<float>().swap(g.xyz);
+            std::vector<float>().swap(g.bxyz);
+            std::vector<float>().swap(g.bnrm);
+            std::vector<uint32_t>().swap(g.tris);
+        }
+        finalized = true;
+        return sync();
+    }
+
+    int variant() const {
+        int v = 0;
+        if (perk) v |= SV_PERK;
+        if (p.verlet_damping == 1.0f) v |= SV_REFV;
+        if (p.collide && any_body) v |= SV_COLLIDE;
+        if (p.check_every > 0) v |= SV_CHECK;
+        return v;
+    }
+
+    StepParams step_params() const {
+        StepParams sp;
+        sp.dt = p.dt;
+        sp.mass = p.mass;
+        sp.gx = p.gravity[0];
+        sp.gy = p.gravity[1];
+        sp.gz = p.gravity[2];
+        sp.damp = p.force_damping;
+        sp.kd = p.spring_damping;
+        sp.gamma = p.verlet_damping;
+        for (int l = 0; l < VISG_MAX_LISTS; ++l) sp.list_k[l] = p.list_k[l];
+        sp.n_lists = p.n_lists;
+        sp.max_disp = p.max_displacement;
+        return sp;
+    }
+
+    StepArgs args(int from, int blk) const {
+        StepArgs a;
+        a.state_in = d_state[from];
+        a.state_out = d_state[from ^ 1];
+        a.normal = d_normal;
+        a.rowp = d_rowp;
+        a.ent = d_ent;
+        a.kent = d_k;
+        int bi = block_index(blk);
+        a.tiles = d_tiles[bi];
+        a.n_tiles = n_tiles[bi];
+        a.bodies = d_views;
+        a.err = d_err;
+        a.check = d_check;
+        a.p = step_params();
+        return a;
+    }
+
+    cudaError_t launch_one(cudaStream_t s, int from) { return launch_step(args(from, block), variant(), block, grid, s); }
+
+    int capture_chunk(int c) {
+        cudaGraph_t g = nullptr;
+        CU(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        int from = c;
+        cudaError_t le = cudaSuccess;
+        for (int k = 0; k < chunk_steps; ++k) {
+            cudaError_t e = launch_one(cap, from);
+            if (e != cudaSuccess && le == cudaSuccess) le = e;
+            from ^= 1;
+        }
+        cudaError_t ee = cudaStreamEndCapture(cap, &g);
+        if (le != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(le, "step capture");
+        }
+        CU(ee);
+        cudaError_t ie = cudaGraphInstantiate(&chunk_exec[c], g, 0);
+        cudaGraphDestroy(g);
+        CU(ie);
+        return VISG_OK;
+    }
+
+    int step(int n) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (n < 0) return fail(VISG_ERR_INVALID_ARG, "nsteps < 0");
+        while (n > 0) {
+            if (p.use_graph && n >= chunk_steps) {
+                if (!chunk_exec[cur]) {
+                    int r = capture_chunk(cur);
+                    if (r) return r;
+                }
+                CU(cudaGraphLaunch(chunk_exec[cur], stream));
+                n -= chunk_steps;
+                steps_since_check += chunk_steps;
+            } else {
+                CU(launch_one(stream, cur));
+                cur ^= 1;
+                --n;
+                ++steps_since_check;
+            }
+            if (p.check_every > 0 && steps_since_check >= p.check_every) {
+                steps_since_check = 0;
+                int r = sync();
+                if (r) return r;
+            }
+        }
+        return VISG_OK;
+    }
+
+    // wait, then report device-side errors (and the divergence check)
+    int sync() {
+        CU(cudaMemcpyAsync(h_status, d_err, 4, cudaMemcpyDeviceToHost, stream));
+        CU(cudaMemcpyAsync(h_status + 1, d_check, 8, cudaMemcpyDeviceToHost, stream));
+        CU(cudaStreamSynchronize(stream));
+        uint32_t err = h_status[0];
+        float maxd;
+        std::memcpy(&maxd, &h_status[1], 4);
+        uint32_t bad = h_status[2];
+        if (err || bad || (p.check_every > 0 && maxd > p.max_displacement)) {
+            CU(cudaMemsetAsync(d_err, 0, 4, stream));
+            CU(cudaMemsetAsync(d_check, 0, 8, stream));
+            CU(cudaStreamSynchronize(stream));
+            if (err & ERR_TIMEOUT) return fail(VISG_ERR_TIMEOUT, "a bounded device wait gave up (LBVH look-back)");
+            if (err & ERR_STACK) return fail(VISG_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+            char buf[160];
+            std::snprintf(buf, sizeof buf, "diverged: %u non-finite vertices, max step displacement %g (limit %g)", bad,
+                          (double)maxd, (double)p.max_displacement);
+            return fail(VISG_ERR_DIVERGED, buf);
+        }
+        if (p.check_every > 0) CU(cudaMemsetAsync(d_check, 0, 8, stream));
+        return VISG_OK;
+    }
+
+    int body_build(int g) {
+        if (p.use_graph) {
+            if (!body_exec[g]) {
+                cudaGraph_t gr = nullptr;
+                CU(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+                cudaError_t le = lbvh_build(bvh[g], p.thickness, p.box_depth, d_err, cap);
+                cudaError_t ee = cudaStreamEndCapture(cap, &gr);
+                if (le != cudaSuccess) {
+                    if (gr) cudaGraphDestroy(gr);
+                    return cuda_fail(le, "LBVH capture");
+                }
+                CU(ee);
+                cudaError_t ie = cudaGraphInstantiate(&body_exec[g], gr, 0);
+                cudaGraphDestroy(gr);
+                CU(ie);
+            }
+            CU(cudaGraphLaunch(body_exec[g], stream));
+        } else {
+            CU(lbvh_build(bvh[g], p.thickness, p.box_depth, d_err, stream));
+        }
+        return VISG_OK;
+    }
+
+    int update_body(int g, const float* xyz, const float* nrm, cudaMemcpyKind kind) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (g < 0 || g >= G) return fail(VISG_ERR_INVALID_ARG, "garment out of range");
+        if (gin[g].nt == 0) return fail(VISG_ERR_STATE, "garment has no body");
+        if (!xyz) return fail(VISG_ERR_INVALID_ARG, "body_xyz is NULL");
+        if ((nrm != nullptr) != bvh[g].has_normals)
+            return fail(VISG_ERR_INVALID_ARG, "body normals must be given iff they were given at creation");
+        CU(cudaMemcpyAsync(bvh[g].xyz_in, xyz, (size_t)bvh[g].nv * 12, kind, stream));
+        if (nrm) CU(cudaMemcpyAsync(bvh[g].nrm_in, nrm, (size_t)bvh[g].nv * 12, kind, stream));
+        return body_build(g);
+    }
+
+    int check_vertex(int g, uint32_t idx, int64_t* v) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (g < 0 || g >= G) return fail(VISG_ERR_INVALID_ARG, "garment out of range");
+        if (idx >= (uint32_t)gin[g].N) return fail(VISG_ERR_INVALID_ARG, "vertex index out of range");
+        *v = voff[g] + idx;
+        return VISG_OK;
+    }
+
+    int set_vertex(int g, uint32_t idx, const float* xyz) {
+        int64_t v;
+        if (int r = check_vertex(g, idx, &v)) return r;
+        if (!xyz) return fail(VISG_ERR_INVALID_ARG, "xyz is NULL");
+        float rec[6] = {xyz[0], xyz[1], xyz[2], xyz[0], xyz[1], xyz[2]};  // x and x_old (simulation.cu:255-256)
+        CU(cudaMemcpyAsync(&d_state[cur][2 * v], rec, sizeof rec, cudaMemcpyHostToDevice, stream));
+        CU(cudaStreamSynchronize(stream));
+        return VISG_OK;
+    }
+
+    int set_pinned(const uint32_t* idx, int n) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (n < 0 || (n > 0 && !idx)) return fail(VISG_ERR_INVALID_ARG, "bad pin list");
+        for (int k = 0; k < n; ++k)
+            if (idx[k] >= (uint32_t)N) return fail(VISG_ERR_INVALID_ARG, "pinned index out of range");
+        for (int64_t i = 0; i < N; ++i) h_rowp[i] &= ROW_MASK;
+        for (int k = 0; k < n; ++k) h_rowp[idx[k]] |= PIN_BIT;
+        CU(cudaMemcpyAsync(d_rowp, h_rowp.data(), (size_t)N * 4, cudaMemcpyHostToDevice, stream));
+        CU(cudaStreamSynchronize(stream));
+        return VISG_OK;
+    }
+
+    int get_positions(int g, float* out, int on_device) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
+        int64_t v0 = 0, n = N;
+        if (g >= 0) {
+            if (g >= G) return fail(VISG_ERR_INVALID_ARG, "garment out of range");
+            v0 = voff[g];
+            n = voff[g + 1] - voff[g];
+        }
+        if (on_device) {
+            CU(launch_unpack_positions(d_state[cur] + 2 * v0, n, out, stream));
+            return VISG_OK;
+        }
+        CU(launch_unpack_positions(d_state[cur] + 2 * v0, n, d_stage, stream));
+        CU(cudaMemcpyAsync(out, d_stage, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
+        return sync();
+    }
+
+    int get_state(float* x, float* xo, float* nrm) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        float* sx = d_stage;
+        float* sxo = d_stage + 3 * N;
+        float* sn = d_stage + 6 * N;
+        CU(launch_unpack_state(d_state[cur], d_normal, N, sx, sxo, sn, stream));
+        if (x) CU(cudaMemcpyAsync(x, sx, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
+        if (xo) CU(cudaMemcpyAsync(xo, sxo, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
+        if (nrm) CU(cudaMemcpyAsync(nrm, sn, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
+        return sync();
+    }
+
+    int set_state(const float* x, const float* xo, const float* nrm) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        float* sx = d_stage;
+        float* sxo = d_stage + 3 * N;
+        float* sn = d_stage + 6 * N;
+        if (x) CU(cudaMemcpyAsync(sx, x, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+        if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+        if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
+        CU(launch_pack_state(d_state[cur], d_normal, N, x ? sx : nullptr, xo ? sxo : nullptr, nrm ? sn : nullptr,
+                             stream));
+        CU(cudaStreamSynchronize(stream));
+        return VISG_OK;
+    }
+
+    int export_lbvh(int g, uint32_t* tri_codes, float* tri_boxes, uint32_t* sorted_codes, int32_t* sorted_tris,
+                    int32_t* child_a, int32_t* child_b, int32_t* parent_int, int32_t* parent_leaf, float* int_boxes,
+                    float* leaf_boxes, float* root_box) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (int r = sync()) return r;
+        const BvhBuffers& b = bvh[g];
+        const int T = gin[g].nt;
+        if (T == 0) return VISG_OK;
+        BvhRoot rt;
+        CU(cudaMemcpy(&rt, b.root, sizeof rt, cudaMemcpyDeviceToHost));
+        const int Tp = rt.n_leaves;
+        std::vector<uint32_t> codes(T), ucode(Tp), utri(Tp);
+        std::vector<float4> tb(2 * (size_t)T);
+        CU(cudaMemcpy(codes.data(), b.codes, T * 4, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(tb.data(), b.tri_box, tb.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(ucode.data(), b.ucode, Tp * 4, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(utri.data(), b.utri, Tp * 4, cudaMemcpyDeviceToHost));
+        auto put = [](float* dst, float4 lo, float4 hi) {
+            dst[0] = lo.x; dst[1] = lo.y; dst[2] = lo.z; dst[3] = hi.x; dst[4] = hi.y; dst[5] = hi.z;
+        };
+        for (int t = 0; t < T; ++t) {
+            if (tri_codes) tri_codes[t] = codes[t];
+            if (tri_boxes) put(tri_boxes + 6 * t, tb[2 * t], tb[2 * t + 1]);
+        }
+        for (int i = 0; i < Tp; ++i) {
+            if (sorted_codes) sorted_codes[i] = ucode[i];
+            if (sorted_tris) sorted_tris[i] = (int32_t)utri[i];
+        }
+        if (root_box) put(root_box, rt.frame_lo, rt.frame_hi);
+        if (Tp == 1) {
+            if (parent_leaf) parent_leaf[0] = 0;
+            if (leaf_boxes) put(leaf_boxes, rt.top_lo, rt.top_hi);
+            return VISG_OK;
+        }
+        const int ni = Tp - 1;
+        std::vector<Node> nd(ni);
+        std::vector<int2> rg(ni);
+        CU(cudaMemcpy(nd.data(), b.nodes, ni * sizeof(Node), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(rg.data(), b.range, ni * sizeof(int2), cudaMemcpyDeviceToHost));
+        // renumber split-indexed nodes into the reference's layout: the root is 0, an
+        // internal node that is child A has the index of its last leaf, child B of its first
+        std::vector<int> kidx(ni, -1);
+        kidx[rt.root] = 0;
+        auto link = [](float w) {
+            int v;
+            std::memcpy(&v, &w, 4);
+            return v;
+        };
+        for (int gg = 0; gg < ni; ++gg) {
+            int la = link(nd[gg].a_lo.w), lb = link(nd[gg].b_lo.w);
+            if (la >= 0) kidx[la] = rg[la].y;
+            if (lb >= 0) kidx[lb] = rg[lb].x;
+        }
+        for (int gg = 0; gg < ni; ++gg)
+            if (kidx[gg] < 0 || kidx[gg] >= ni) return fail(VISG_ERR_CUDA, "LBVH export: inconsistent tree");
+        std::vector<int32_t> ca(ni, 0), cb(ni, 0), pi(ni, 0), pl(Tp, 0);
+        std::vector<float> ib(6 * (size_t)ni, 0.0f), lb6(6 * (size_t)Tp, 0.0f);
+        put(&ib[0], rt.top_lo, rt.top_hi);  // root box (identity U A U B)
+        for (int gg = 0; gg < ni; ++gg) {
+            const int k = kidx[gg];
+            const int la = link(nd[gg].a_lo.w), lbk = link(nd[gg].b_lo.w);
+            if (la < 0) {
+                ca[k] = -(~la) - 1;
+                pl[~la] = k + 1;
+                put(&lb6[6 * (size_t)(~la)], nd[gg].a_lo, nd[gg].a_hi);
+            } else {
+                ca[k] = kidx[la] + 1;
+                pi[kidx[la]] = k + 1;
+                put(&ib[6 * (size_t)kidx[la]], nd[gg].a_lo, nd[gg].a_hi);
+            }
+            if (lbk < 0) {
+                cb[k] = -(~lbk) - 1;
+                pl[~lbk] = k + 1;
+                put(&lb6[6 * (size_t)(~lbk)], nd[gg].b_lo, nd[gg].b_hi);
+            } else {
+                cb[k] = kidx[lbk] + 1;
+                pi[kidx[lbk]] = k + 1;
+                put(&ib[6 * (size_t)kidx[lbk]], nd[gg].b_lo, nd[gg].b_hi);
+            }
+        }
+        if (child_a) std::memcpy(child_a, ca.data(), ni * 4);
+        if (child_b) std::memcpy(child_b, cb.data(), ni * 4);
+        if (parent_int) std::memcpy(parent_int, pi.data(), ni * 4);
+        if (parent_leaf) std::memcpy(parent_leaf, pl.data(), Tp * 4);
+        if (int_boxes) std::memcpy(int_boxes, ib.data(), ib.size() * 4);
+        if (leaf_boxes) std::memcpy(leaf_boxes, lb6.data(), lb6.size() * 4);
+        return VISG_OK;
+    }
+
+    int query(int g, const float* pts, int n, int32_t* leaf, int32_t* inside, float* dist, float* normal) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (n < 0 || (n > 0 && !pts)) return fail(VISG_ERR_INVALID_ARG, "bad points");
+        if (n == 0) return VISG_OK;
+        if (gin[g].nt == 0) {
+            for (int i = 0; i < n; ++i) {
+                if (leaf) leaf[i] = -1;
+                if (inside) inside[i] = 0;
+                if (dist) dist[i] = 0.0f;
+                if (normal) normal[3 * i] = normal[3 * i + 1] = normal[3 * i + 2] = 0.0f;
+            }
+            return VISG_OK;
+        }
+        char* buf = nullptr;
+        size_t bytes = (size_t)n * (12 + 4 + 4 + 4 + 12);
+        CU(cudaMalloc((void**)&buf, bytes));
+        float* dp = (float*)buf;
+        int* dl = (int*)(dp + 3 * (size_t)n);
+        int* di = dl + n;
+        float* dd = (float*)(di + n);
+        float* dn = dd + n;
+        cudaError_t e = cudaMemcpyAsync(dp, pts, (size_t)n * 12, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = launch_query(bvh[g].view(), dp, n, dl, di, dd, dn, d_err, stream);
+        if (e == cudaSuccess && leaf) e = cudaMemcpyAsync(leaf, dl, n * 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess && inside) e = cudaMemcpyAsync(inside, di, n * 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess && dist) e = cudaMemcpyAsync(dist, dd, n * 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess && normal) e = cudaMemcpyAsync(normal, dn, (size_t)n * 12, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        cudaFree(buf);
+        if (e != cudaSuccess) return cuda_fail(e, "query");
+        return sync();
+    }
+
+    // time every launch shape on this engine's data; keep the fastest; restore the state
+    int autotune(int* out_block, int* out_ctas) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (int r = sync()) return r;
+        float4 *bs = nullptr, *bn = nullptr;
+        CU(cudaMalloc((void**)&bs, 2 * (size_t)N * sizeof(float4)));
+        cudaError_t e = cudaMalloc((void**)&bn, (size_t)N * sizeof(float4));
+        if (e != cudaSuccess) {
+            cudaFree(bs);
+            return cuda_fail(e, "autotune backup");
+        }
+        const int cur0 = cur;
+        e = cudaMemcpyAsync(bs, d_state[cur], 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(bn, d_normal, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 1e30f;
+        int best_block = block, best_grid = grid, best_ctas = 0;
+        for (int bi = 0; bi < 3 && e == cudaSuccess; ++bi) {
+            const int blk = kBlocks[bi];
+            const int occ = step_max_ctas_per_sm(variant(), blk);
+            std::vector<int> ctas;
+            for (int c = 1; c <= occ; c *= 2) ctas.push_back(c);
+            if (occ > 0 && ctas.back() != occ) ctas.push_back(occ);
+            ctas.push_back(0);  // one tile per CTA
+            for (int c : ctas) {
+                const int gr = c == 0 ? 0 : c * sm_count;
+                auto run = [&](int k) {
+                    for (int s = 0; s < k && e == cudaSuccess; ++s) {
+                        e = launch_step(args(cur, blk), variant(), blk, gr, stream);
+                        cur ^= 1;
+                    }
+                };
+                run(1);
+                cudaEventRecord(e0, stream);
+                run(4);
+                cudaEventRecord(e1, stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (e == cudaSuccess && ms < best) {
+                    best = ms;
+                    best_block = blk;
+                    best_grid = gr;
+                    best_ctas = c;
+                }
+            }
+        }
+        cur = cur0;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_state[cur], bs, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_normal, bn, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(bs);
+        cudaFree(bn);
+        if (e != cudaSuccess) return cuda_fail(e, "autotune");
+        if (best_block != block || best_grid != grid) {
+            block = best_block;
+            grid = best_grid;
+            destroy_graphs();
+        }
+        if (out_block) *out_block = block;
+        if (out_ctas) *out_ctas = best_ctas;
+        return sync();
+    }
+
+    int forward(int nsteps, int ckpt);
+    int backward(const float* dL_dx, const float* dL_dxo, float* dL_dk, float* dL_dscalar);
+};
+
+struct VisgSim {
+    Engine eng;
+};
+struct VisgBatch {
+    Engine eng;
+};
+
+#include "visg_adjoint_host.inl"
+
+// =====================================================================================
+extern "C" {
+
+void visg_default_params(VisgParams* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->dt = 1.0f / 40.0f;
+    p->mass = 0.3f;
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -0.00981f;
+    p->gravity[2] = 0.0f;
+    p->force_damping = -0.02f;
+    p->spring_damping = -0.5f;
+    p->verlet_damping = 1.0f;
+    p->thickness = 0.003f;
+    p->box_depth = 0.01f;
+    p->n_lists = 2;
+    p->list_k[0] = 100.0f;
+    p->list_k[1] = 2.0f;
+    p->list_k[2] = 2.0f;
+    p->list_k[3] = 2.0f;
+    p->collide = 1;
+    p->check_every = 0;
+    p->max_displacement = 1.0f;
+    p->use_graph = 1;
+}
+
+const char* visg_version(void) { return "visg-gb300 1.0 (sm_103a)"; }
+const char* visg_last_error(void) { return g_err.c_str(); }
+
+static int ensure_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(VISG_ERR_NO_DEVICE, "no CUDA device visible");
+    return VISG_OK;
+}
+
+int visg_create(const VisgParams* params, const float* cloth_xyz, int32_t n_vertices, const uint32_t* const* csr_row,
+                const VisgSpring* const* csr, const float* const* list_k, const float* body_xyz,
+                const float* body_normals, int32_t n_body_vertices, const uint32_t* tris, int32_t n_tris,
+                VisgSim** out) {
+    if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (int r = validate_params(params)) return r;
+    if (int r = ensure_device()) return r;
+    auto* s = new VisgSim();
+    s->eng.p = *params;
+    int r = s->eng.add(cloth_xyz, n_vertices, csr_row, csr, list_k, nullptr, 0, body_xyz, body_normals,
+                       n_body_vertices, tris, n_tris, nullptr);
+    if (r == VISG_OK) r = s->eng.finalize();
+    if (r != VISG_OK) {
+        std::string m = g_err;
+        delete s;
+        g_err = m;
+        return r;
+    }
+    *out = s;
+    return VISG_OK;
+}
+
+int visg_destroy(VisgSim* sim) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    delete sim;
+    return VISG_OK;
+}
+
+int visg_set_stream(VisgSim* sim, void* stream) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    sim->eng.stream = (cudaStream_t)stream;
+    return VISG_OK;
+}
+
+int visg_step(VisgSim* sim, int32_t nsteps) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.step(nsteps);
+}
+
+int visg_update_body(VisgSim* sim, const float* xyz, const float* nrm) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.update_body(0, xyz, nrm, cudaMemcpyHostToDevice);
+}
+
+int visg_update_body_device(VisgSim* sim, const float* xyz, const float* nrm) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.update_body(0, xyz, nrm, cudaMemcpyDeviceToDevice);
+}
+
+int visg_set_vertex(VisgSim* sim, uint32_t idx, const float xyz[3]) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.set_vertex(0, idx, xyz);
+}
+
+int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.set_pinned(idx, n);
+}
+
+int visg_get_positions(VisgSim* sim, float* out, int32_t on_device) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.get_positions(0, out, on_device);
+}
+
+int visg_get_state(VisgSim* sim, float* x, float* xo, float* n) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.get_state(x, xo, n);
+}
+
+int visg_set_state(VisgSim* sim, const float* x, const float* xo, const float* n) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.set_state(x, xo, n);
+}
+
+int visg_sync(VisgSim* sim) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.sync();
+}
+
+int visg_get_info(VisgSim* sim, int32_t* nv, int32_t* ne, int32_t* nt, int32_t* nl) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    Engine& e = sim->eng;
+    if (nv) *nv = (int32_t)e.N;
+    if (ne) *ne = (int32_t)e.E;
+    if (nt) *nt = e.gin[0].nt;
+    if (nl) {
+        *nl = 0;
+        if (e.gin[0].nt > 0) {
+            if (int r = e.sync()) return r;
+            BvhRoot rt;
+            cudaError_t ce = cudaMemcpy(&rt, e.bvh[0].root, sizeof rt, cudaMemcpyDeviceToHost);
+            if (ce != cudaSuccess) return cuda_fail(ce, "info");
+            *nl = rt.n_leaves;
+        }
+    }
+    return VISG_OK;
+}
+
+int visg_export_lbvh(VisgSim* sim, uint32_t* tri_codes, float* tri_boxes, uint32_t* sorted_codes, int32_t* sorted_tris,
+                     int32_t* child_a, int32_t* child_b, int32_t* parent_internal, int32_t* parent_leaf,
+                     float* internal_boxes, float* leaf_boxes, float* root_box) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.export_lbvh(0, tri_codes, tri_boxes, sorted_codes, sorted_tris, child_a, child_b, parent_internal,
+                                parent_leaf, internal_boxes, leaf_boxes, root_box);
+}
+
+int visg_query_points(VisgSim* sim, const float* pts, int32_t n, int32_t* leaf, int32_t* inside, float* dist,
+                      float* normal) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.query(0, pts, n, leaf, inside, dist, normal);
+}
+
+int visg_forward(VisgSim* sim, int32_t nsteps, int32_t ckpt) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.forward(nsteps, ckpt);
+}
+
+int visg_backward(VisgSim* sim, const float* dL_dx, const float* dL_dxo, float* dL_dk, float* dL_dscalar) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.backward(dL_dx, dL_dxo, dL_dk, dL_dscalar);
+}
+
+// ---------------------------------------------------------------------------------------
+int visg_batch_create(const VisgParams* params, VisgBatch** out) {
+    if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (int r = validate_params(params)) return r;
+    if (int r = ensure_device()) return r;
+    auto* b = new VisgBatch();
+    b->eng.p = *params;
+    *out = b;
+    return VISG_OK;
+}
+
+int visg_batch_add(VisgBatch* b, const float* cloth_xyz, int32_t n_vertices, const uint32_t* const* csr_row,
+                   const VisgSpring* const* csr, const float* const* list_k, const uint32_t* pinned, int32_t n_pinned,
+                   const float* body_xyz, const float* body_normals, int32_t n_body_vertices, const uint32_t* tris,
+                   int32_t n_tris, int32_t* garment) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    if (n_pinned < 0 || (n_pinned > 0 && !pinned)) return fail(VISG_ERR_INVALID_ARG, "bad pin list");
+    return b->eng.add(cloth_xyz, n_vertices, csr_row, csr, list_k, pinned, n_pinned, body_xyz, body_normals,
+                      n_body_vertices, tris, n_tris, garment);
+}
+
+int visg_batch_finalize(VisgBatch* b) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.finalize();
+}
+
+int visg_batch_set_stream(VisgBatch* b, void* stream) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    b->eng.stream = (cudaStream_t)stream;
+    return VISG_OK;
+}
+
+int visg_batch_step(VisgBatch* b, int32_t nsteps) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.step(nsteps);
+}
+
+int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.get_positions(garment, out, on_device);
+}
+
+int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.set_vertex(garment, idx, xyz);
+}
+
+int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* xyz, const float* nrm) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.update_body(garment, xyz, nrm, cudaMemcpyHostToDevice);
+}
+
+int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.autotune(block, ctas);
+}
+
+int visg_batch_info(VisgBatch* b, int32_t* ng, int64_t* nv, int64_t* ne, int64_t* nt) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    Engine& e = b->eng;
+    if (ng) *ng = (int32_t)e.gin.size();
+    if (nv) *nv = e.N;
+    if (ne) {
+        int64_t s = 0;
+        for (auto& g : e.gin)
+            for (auto& r : g.rows) s += r.back();
+        *ne = s;
+    }
+    if (nt) {
+        int64_t s = 0;
+        for (auto& g : e.gin) s += g.nt;
+        *nt = s;
+    }
+    return VISG_OK;
+}
+
+int visg_batch_sync(VisgBatch* b) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    if (!b->eng.finalized) return VISG_OK;
+    return b->eng.sync();
+}
+
+int visg_batch_destroy(VisgBatch* b) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    delete b;
+    return VISG_OK;
+}
+
+}  // extern "C"

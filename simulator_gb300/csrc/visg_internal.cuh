@@ -1,0 +1,172 @@
+// visg_internal.cuh — device data layout and host-side engine of the cloth step.
+//
+// HBM layout (all arrays 16-byte aligned, one allocation per engine):
+//   cloth state, double-buffered: 2 float4 per vertex
+//        [x.x x.y x.z xo.x] [xo.y xo.z flags 0]          32 B, one sector per gather
+//   contact normal (previous step):  float4 per vertex, read only when flags says so
+//   rowp:   u32 per vertex + 1, merged CSR row offsets; bit 31 = vertex pinned
+//   ent:    uint2 per directed spring {end | list << 30, rest}         8 B
+//   kent:   f32 per directed spring, only with per-spring stiffness
+//   tiles:  int4 per tile {garment, first vertex, end vertex, 0}; a tile never
+//           straddles two garments
+//   per body: LBVH nodes (64 B: both children's boxes and links), leaves (32 B:
+//           v0 and the face normal), root record; build scratch (sort buffers,
+//           look-back status words, handshake flags)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/visg_sim.h"
+#include "visg_math.cuh"
+
+namespace visg {
+
+constexpr uint32_t PIN_BIT = 0x80000000u;
+constexpr uint32_t ROW_MASK = 0x7fffffffu;
+constexpr uint32_t END_MASK = 0x3fffffffu;
+constexpr int LIST_SHIFT = 30;
+constexpr uint32_t FLAG_HAS_NORMAL = 1u;
+
+// error bits written by kernels into the engine's error word
+constexpr int ERR_STACK = 1;     // traversal stack would overflow (not reachable for <= 30-bit codes)
+constexpr int ERR_DIVERGED = 2;  // divergence check tripped
+constexpr int ERR_TIMEOUT = 4;   // a bounded look-back wait gave up
+
+// LBVH internal node: children's boxes and links.  Links: >= 0 internal node,
+// < 0 leaf ~link.  Each child writes its own two float4 during the build.
+struct __align__(16) Node {
+    float4 a_lo;  // child A min xyz, w = link A
+    float4 a_hi;  // child A max xyz
+    float4 b_lo;  // child B min xyz, w = link B
+    float4 b_hi;  // child B max xyz
+};
+
+struct __align__(16) BvhRoot {
+    int root;      // root internal node, -1 when there are fewer than two leaves
+    int n_leaves;  // T' (after de-duplication)
+    int n_tris;    // T
+    int pad;
+    float4 frame_lo, frame_hi;  // Morton frame: identity box U every expanded triangle box
+    float4 top_lo, top_hi;      // box of the root node (identity U children), or of the only leaf
+    uint32_t acc[8];            // order-preserving accumulators of the frame (min xyz, max xyz)
+};
+
+// device view of one body's LBVH, as the step and query kernels use it
+struct BvhView {
+    const Node* nodes;
+    const float4* leaves;  // 2 per leaf: (v0.xyz, n.x) (n.y, n.z, triangle, 0)
+    const BvhRoot* root;
+};
+
+// ---- host: simple bump allocator over one cudaMalloc --------------------------------
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0, used = 0;
+    std::vector<std::pair<void**, size_t>> plan;
+    template <typename T>
+    void want(T** p, size_t count) { plan.push_back({(void**)p, ((count * sizeof(T) + 255) / 256) * 256}); }
+    cudaError_t commit();
+    void release();
+};
+
+// ---- LBVH buffers of one body ----------------------------------------------------------
+struct BvhBuffers {
+    int nv = 0, nt = 0;        // body vertices, triangles
+    int tiles_sort = 0;        // look-back tiles of one radix pass
+    bool has_normals = false;
+    float* xyz_in = nullptr;   // nv*3 staging (upload target)
+    float* nrm_in = nullptr;   // nv*3 staging
+    float4* verts = nullptr;   // nv, thickness push applied
+    uint32_t* tris = nullptr;  // nt*3
+    float4* tri_box = nullptr;   // 2*nt (min, max)
+    float4* tri_leaf = nullptr;  // 2*nt (v0, n)
+    uint32_t* codes = nullptr;   // nt, per triangle
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* vals[2] = {nullptr, nullptr};
+    uint32_t* ucode = nullptr;   // T'
+    uint32_t* utri = nullptr;    // T'
+    Node* nodes = nullptr;       // nt-1
+    float4* leaves = nullptr;    // 2*nt
+    uint32_t* flags = nullptr;   // nt-1 handshake counters (self-resetting)
+    int2* range = nullptr;       // nt-1 leaf range of each internal node
+    BvhRoot* root = nullptr;
+    uint32_t* scratch = nullptr; // zeroed before every build (histograms, status words)
+    size_t scratch_words = 0;
+
+    void plan(Arena& a, int nv_, int nt_, bool normals);
+    BvhView view() const { return BvhView{nodes, leaves, root}; }
+};
+
+// Launch the full device build: vertex push -> boxes + frame -> Morton codes + digit
+// histograms -> 4 radix passes -> de-duplication -> bottom-up build + refit.
+cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s);
+
+// ---- step kernel arguments ---------------------------------------------------------------
+struct StepParams {
+    float dt, mass, gx, gy, gz, damp, kd, gamma;
+    float list_k[VISG_MAX_LISTS];
+    int n_lists;
+    float max_disp;
+};
+
+struct StepArgs {
+    const float4* state_in;
+    float4* state_out;
+    float4* normal;  // in place
+    const uint32_t* rowp;
+    const uint2* ent;
+    const float* kent;
+    const int4* tiles;
+    int n_tiles;
+    const BvhView* bodies;  // per garment
+    int* err;
+    uint32_t* check;  // [0] max |dx| bits, [1] non-finite count
+    StepParams p;
+};
+
+enum StepVariant : int {
+    SV_PERK = 1,      // per-spring stiffness array
+    SV_REFV = 2,      // reference Verlet expression (gamma == 1)
+    SV_COLLIDE = 4,   // body collision
+    SV_CHECK = 8,     // divergence check
+};
+cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
+int step_max_ctas_per_sm(int variant, int block);
+
+// first-hit queries of external points against one body
+cudaError_t launch_query(BvhView v, const float* pts, int n, int* leaf, int* inside, float* dist,
+                         float* normal, int* err, cudaStream_t s);
+
+// unpack positions of vertices [0, n) into packed xyz
+cudaError_t launch_unpack_positions(const float4* state, int64_t n, float* out, cudaStream_t s);
+cudaError_t launch_unpack_state(const float4* state, const float4* normal, int64_t n, float* x, float* xo,
+                                float* nrm, cudaStream_t s);
+cudaError_t launch_pack_state(float4* state, float4* normal, int64_t n, const float* x, const float* xo,
+                              const float* nrm, cudaStream_t s);
+
+// ---- adjoint ---------------------------------------------------------------------------
+struct AdjArgs {
+    const float4* state;    // the step's input state (x, x_old, flags)
+    const float4* normal_in;  // contact normals entering the step (frozen projection)
+    const float4* hit;      // per vertex: projection normal of this step (w = 1 if projected)
+    const uint32_t* rowp;
+    const uint2* ent;
+    const float* kent;
+    const uint32_t* rev;    // reverse entry of every directed spring
+    const float4* lam_in;   // 2 per vertex: adjoint of (x', x_old') of the step's outputs
+    float4* lam_out;        // 2 per vertex: adjoint of (x, x_old)
+    float4* G;              // per vertex: adjoint of the force
+    float* dk;              // per entry, accumulated
+    double* dscalar;        // [3] accumulated (gamma, force damping, kd)
+    int n;
+    StepParams p;
+};
+cudaError_t launch_adjoint_step(const AdjArgs& a, cudaStream_t s);
+// forward step that also records, per vertex, the projection normal (w = 1 when projected)
+cudaError_t launch_record_hits(const float4* state_out, const float4* normal, int64_t n, float4* hit,
+                               cudaStream_t s);
+
+}  // namespace visg

@@ -1,0 +1,511 @@
+// visg_lbvh.cu — per-step body LBVH build on the device.
+//
+// Reference (BVHAccel, src/bvh/bvh.cu:154-297; cudaBRT.cu:9-206) builds once per
+// body with a device->host->device round trip: expanded boxes and Morton codes on
+// the GPU, std::sort + duplicate removal on the CPU, then Karras internal nodes and
+// an atomic-counter refit on the GPU.  Here the whole build stays on the device,
+// in nine stream-ordered kernels, so it can run every step and be captured in a
+// CUDA graph:
+//   k_body_prep   vertex_extend (Mesh.cpp:101-117): v += thickness * n
+//   k_tri_boxes   expanded triangle boxes (primitive.cu:79-91) + the Morton frame
+//                 (identity box U all boxes) by warp-shuffle min/max reduction
+//   k_morton      Morton code of each box centroid in the frame (bvh.cu:20-41,71-79;
+//                 bbox.h:97-127) + the digit histograms of all four radix passes
+//   k_sort_pass   x4: stable LSD radix pass, 8-bit digits, decoupled look-back
+//                 (ties keep triangle order, i.e. sort by (code, triangle))
+//   k_unique      keep the first triangle of every distinct code
+//                 (remove_redundant, Utilities.h:35-55), look-back compaction
+//   k_build       bottom-up radix-tree build fused with the refit: each leaf thread
+//                 climbs, the parent of range [l, r] is the boundary with the longer
+//                 common prefix (delta(l-1,l) vs delta(r,r+1), delta = clz(a ^ b) as
+//                 cudaBRT.cu:9-19), the second child to arrive merges both boxes into
+//                 the identity box (calculateBoudingBox, cudaBRT.cu:166-206) and
+//                 continues.  Nodes are numbered by their split position; the tree is
+//                 the same binary radix tree processInternalNode (cudaBRT.cu:120-161)
+//                 builds, and visg_export_lbvh renumbers it into the reference's layout.
+// Every wait is bounded; a wait that gives up sets ERR_TIMEOUT and the host reports
+// VISG_ERR_TIMEOUT.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "visg_internal.cuh"
+
+namespace visg {
+
+namespace {
+
+constexpr int BUILD_THREADS = 256;
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_ITEMS = 8;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 2048
+constexpr int RADIX = 256;
+constexpr int PASSES = 4;
+constexpr uint32_t ST_AGG = 1u << 30;
+constexpr uint32_t ST_PREFIX = 2u << 30;
+constexpr uint32_t ST_VALUE = (1u << 30) - 1u;
+constexpr int SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
+    return *reinterpret_cast<const volatile uint32_t*>(p);
+}
+__device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *reinterpret_cast<volatile uint32_t*>(p) = v; }
+
+// inclusive scan of one value per thread over a 256-thread block
+__device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) s_warp[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t r = v + (warp > 0 ? s_warp[warp - 1] : 0u);
+    __syncthreads();
+    return r;
+}
+
+// ------------------------------------------------------------------------------------------
+__global__ void k_body_prep(const float* __restrict__ xyz, const float* __restrict__ nrm, int nv, float thickness,
+                            float4* __restrict__ verts, BvhRoot* root, int nt) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v == 0) {
+        root->acc[0] = root->acc[1] = root->acc[2] = f2ord(100.0f);   // identity box min (bbox.h:17-22)
+        root->acc[3] = root->acc[4] = root->acc[5] = f2ord(-100.0f);  // identity box max
+        root->n_tris = nt;
+    }
+    if (v >= nv) return;
+    float x = xyz[3 * v], y = xyz[3 * v + 1], z = xyz[3 * v + 2];
+    if (nrm) {
+        x = __fadd_rn(x, __fmul_rn(thickness, nrm[3 * v]));
+        y = __fadd_rn(y, __fmul_rn(thickness, nrm[3 * v + 1]));
+        z = __fadd_rn(z, __fmul_rn(thickness, nrm[3 * v + 2]));
+    }
+    verts[v] = make_float4(x, y, z, 0.0f);
+}
+
+__device__ __forceinline__ void box_add(f3& lo, f3& hi, f3 p) {
+    lo.x = fminf(lo.x, p.x); lo.y = fminf(lo.y, p.y); lo.z = fminf(lo.z, p.z);
+    hi.x = fmaxf(hi.x, p.x); hi.y = fmaxf(hi.y, p.y); hi.z = fmaxf(hi.z, p.z);
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS)
+k_tri_boxes(const float4* __restrict__ verts, const uint32_t* __restrict__ tris, int nt, float depth,
+            float4* __restrict__ tri_box, float4* __restrict__ tri_leaf, BvhRoot* root) {
+    __shared__ float s_red[6][BUILD_THREADS / 32];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    f3 lo = mk3(100.0f, 100.0f, 100.0f), hi = mk3(-100.0f, -100.0f, -100.0f);
+    if (t < nt) {
+        f3 v0 = xyz(__ldg(&verts[tris[3 * t]]));
+        f3 v1 = xyz(__ldg(&verts[tris[3 * t + 1]]));
+        f3 v2 = xyz(__ldg(&verts[tris[3 * t + 2]]));
+        f3 n = normalize(cross(sub(v1, v0), sub(v2, v0)));  // Primitive::d_get_normal
+        f3 blo = v0, bhi = v0;                                 // BBox(v0).expand(v1).expand(v2)
+        box_add(blo, bhi, v1);
+        box_add(blo, bhi, v2);
+        f3 dn = mul(depth, n);
+        box_add(blo, bhi, sub(v0, dn));
+        box_add(blo, bhi, sub(v1, dn));
+        box_add(blo, bhi, sub(v2, dn));
+        tri_box[2 * t] = make_float4(blo.x, blo.y, blo.z, 0.0f);
+        tri_box[2 * t + 1] = make_float4(bhi.x, bhi.y, bhi.z, 0.0f);
+        tri_leaf[2 * t] = make_float4(v0.x, v0.y, v0.z, n.x);
+        tri_leaf[2 * t + 1] = make_float4(n.y, n.z, __int_as_float(t), 0.0f);
+        lo = blo;
+        hi = bhi;
+    }
+    // frame = identity U every box: block min/max, then one ordered atomic per block
+    float r[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r[k] = fminf(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+#pragma unroll
+        for (int k = 3; k < 6; ++k) r[k] = fmaxf(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < 6; ++k) s_red[k][warp] = r[k];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int k = threadIdx.x;
+        float v = s_red[k][0];
+        for (int w = 1; w < BUILD_THREADS / 32; ++w) v = k < 3 ? fminf(v, s_red[k][w]) : fmaxf(v, s_red[k][w]);
+        if (k < 3) atomicMin(&root->acc[k], f2ord(v));
+        else atomicMax(&root->acc[k], f2ord(v));
+    }
+}
+
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v) {  // bvh.cu:20-27
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS)
+k_morton(const float4* __restrict__ tri_box, int nt, BvhRoot* root, uint32_t* __restrict__ codes,
+         uint32_t* __restrict__ ghist /* PASSES*RADIX */) {
+    __shared__ uint32_t s_hist[PASSES][RADIX];
+    __shared__ float s_frame[6];
+    for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) (&s_hist[0][0])[k] = 0;
+    if (threadIdx.x < 6) s_frame[threadIdx.x] = ord2f(root->acc[threadIdx.x]);
+    __syncthreads();
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        root->frame_lo = make_float4(s_frame[0], s_frame[1], s_frame[2], 0.0f);
+        root->frame_hi = make_float4(s_frame[3], s_frame[4], s_frame[5], 0.0f);
+    }
+    if (t < nt) {
+        float4 lo = tri_box[2 * t], hi = tri_box[2 * t + 1];
+        f3 c = divs(add(xyz(lo), xyz(hi)), 2.0f);  // BBox::centroid
+        f3 fmn = mk3(s_frame[0], s_frame[1], s_frame[2]);
+        f3 ext = sub(mk3(s_frame[3], s_frame[4], s_frame[5]), fmn);
+        f3 q = mk3(0.0f, 0.0f, 0.0f);
+        if (length(ext) != 0.0f) q = divv(sub(c, fmn), ext);  // BBox::getUnitcubePosOf
+        float x = fminf(fmaxf(__fmul_rn(q.x, 1024.0f), 0.0f), 1023.0f);
+        float y = fminf(fmaxf(__fmul_rn(q.y, 1024.0f), 0.0f), 1023.0f);
+        float z = fminf(fmaxf(__fmul_rn(q.z, 1024.0f), 0.0f), 1023.0f);
+        uint32_t code = expand_bits((uint32_t)x) * 4u + expand_bits((uint32_t)y) * 2u + expand_bits((uint32_t)z);
+        codes[t] = code;
+#pragma unroll
+        for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p][(code >> (8 * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) {
+        uint32_t v = (&s_hist[0][0])[k];
+        if (v) atomicAdd(&ghist[k], v);
+    }
+}
+
+// One stable LSD pass over 8-bit digit (key >> shift) & 255.  Tiles are claimed in
+// launch order through an atomic counter, so every tile a block waits on belongs to a
+// block that is already running: the look-back always terminates.
+__global__ void __launch_bounds__(SORT_THREADS)
+k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+            uint32_t* __restrict__ vout, int n, int shift, const uint32_t* __restrict__ ghist,
+            uint32_t* status, uint32_t* counter, int* err) {
+    __shared__ uint32_t s_whist[SORT_THREADS / 32][RADIX + 1];
+    __shared__ uint32_t s_tstart[RADIX];
+    __shared__ uint32_t s_gbase[RADIX];
+    __shared__ uint32_t s_keys[SORT_TILE];
+    __shared__ uint32_t s_vals[SORT_TILE];
+    __shared__ uint32_t s_warp[32];
+    __shared__ int s_tile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = (int)atomicAdd(counter, 1u);
+    for (int k = tid; k < (SORT_THREADS / 32) * (RADIX + 1); k += SORT_THREADS) (&s_whist[0][0])[k] = 0;
+    __syncthreads();
+    const int tile = s_tile;
+    const int base = tile * SORT_TILE + warp * (32 * SORT_ITEMS);
+    uint32_t key[SORT_ITEMS], val[SORT_ITEMS], rank[SORT_ITEMS];
+    int dig[SORT_ITEMS];
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        int idx = base + j * 32 + lane;  // warp-striped: j-major order is input order
+        if (idx < n) {
+            key[j] = kin[idx];
+            val[j] = vin ? vin[idx] : (uint32_t)idx;
+            dig[j] = (int)((key[j] >> shift) & 255u);
+        } else {
+            key[j] = 0u;
+            val[j] = 0u;
+            dig[j] = RADIX;  // padding: own bucket, never written
+        }
+    }
+    // stable rank of every key among equal digits of this warp, in input order
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        uint32_t peers = __match_any_sync(0xffffffffu, dig[j]);
+        int leader = __ffs(peers) - 1;
+        uint32_t before = 0;
+        if (lane == leader) {
+            before = s_whist[warp][dig[j]];
+            s_whist[warp][dig[j]] = before + __popc(peers);
+        }
+        before = __shfl_sync(0xffffffffu, before, leader);
+        rank[j] = before + __popc(peers & ((1u << lane) - 1u));
+        __syncwarp();
+    }
+    __syncthreads();
+    // thread d owns digit d: warp-exclusive prefixes and the tile count
+    const int d = tid;
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < SORT_THREADS / 32; ++w) {
+        uint32_t c = s_whist[w][d];
+        s_whist[w][d] = run;
+        run += c;
+    }
+    const uint32_t tcount = run;
+    const uint32_t tincl = block_scan_incl(tcount, s_warp);
+    s_tstart[d] = tincl - tcount;
+    const uint32_t gh = ghist[d];
+    const uint32_t gincl = block_scan_incl(gh, s_warp);
+    const uint32_t goff = gincl - gh;
+    // publish the tile's count of digit d, then look back for the exclusive prefix
+    uint32_t excl = 0;
+    uint32_t* st = status + (size_t)tile * RADIX + d;
+    if (tile == 0) {
+        st_volatile(st, ST_PREFIX | tcount);
+    } else {
+        st_volatile(st, ST_AGG | tcount);
+        int t = tile - 1;
+        int spins = 0;
+        while (t >= 0) {
+            uint32_t s = ld_volatile(status + (size_t)t * RADIX + d);
+            uint32_t f = s & ~ST_VALUE;
+            if (f == 0u) {
+                if (++spins > SPIN_LIMIT) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            excl += s & ST_VALUE;
+            if (f == ST_PREFIX) break;
+            --t;
+        }
+        st_volatile(st, ST_PREFIX | ((excl + tcount) & ST_VALUE));
+    }
+    s_gbase[d] = goff + excl;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        if (dig[j] < RADIX) {
+            uint32_t pos = s_tstart[dig[j]] + s_whist[warp][dig[j]] + rank[j];
+            s_keys[pos] = key[j];
+            s_vals[pos] = val[j];
+        }
+    }
+    __syncthreads();
+    const int tile_n = min(SORT_TILE, n - tile * SORT_TILE);
+    for (int p = tid; p < tile_n; p += SORT_THREADS) {
+        uint32_t k = s_keys[p];
+        uint32_t dd = (k >> shift) & 255u;
+        uint32_t o = s_gbase[dd] + (uint32_t)p - s_tstart[dd];
+        if (o < (uint32_t)n) {  // always true unless a look-back gave up
+            kout[o] = k;
+            vout[o] = s_vals[p];
+        }
+    }
+}
+
+// keep the first (lowest triangle index) of every run of equal codes
+__global__ void __launch_bounds__(SORT_THREADS)
+k_unique(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int n, uint32_t* __restrict__ ucode,
+         uint32_t* __restrict__ utri, uint32_t* status, uint32_t* counter, int n_tiles, BvhRoot* root, int* err) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_excl;
+    __shared__ int s_tile;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    const int base = tile * SORT_TILE + tid * SORT_ITEMS;
+    uint32_t fl = 0;
+    uint32_t k[SORT_ITEMS];
+    uint32_t prev = base > 0 && base - 1 < n ? keys[base - 1] : 0u;
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        int i = base + j;
+        k[j] = i < n ? keys[i] : 0u;
+        bool first = i < n && (i == 0 || k[j] != prev);
+        fl |= (first ? 1u : 0u) << j;
+        prev = k[j];
+    }
+    const uint32_t cnt = __popc(fl);
+    const uint32_t incl = block_scan_incl(cnt, s_warp);
+    if (tid == SORT_THREADS - 1) {
+        uint32_t tsum = incl;
+        uint32_t excl = 0;
+        uint32_t* st = status + tile;
+        if (tile == 0) {
+            st_volatile(st, ST_PREFIX | tsum);
+        } else {
+            st_volatile(st, ST_AGG | tsum);
+            int t = tile - 1, spins = 0;
+            while (t >= 0) {
+                uint32_t s = ld_volatile(status + t);
+                uint32_t f = s & ~ST_VALUE;
+                if (f == 0u) {
+                    if (++spins > SPIN_LIMIT) {
+                        atomicOr(err, ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                excl += s & ST_VALUE;
+                if (f == ST_PREFIX) break;
+                --t;
+            }
+            st_volatile(st, ST_PREFIX | ((excl + tsum) & ST_VALUE));
+        }
+        s_excl = excl;
+        if (tile == n_tiles - 1) root->n_leaves = (int)min(excl + tsum, (uint32_t)n);
+    }
+    __syncthreads();
+    uint32_t o = s_excl + incl - cnt;
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        if (fl & (1u << j)) {
+            if (o < (uint32_t)n) {  // always true unless a look-back gave up
+                ucode[o] = k[j];
+                utri[o] = vals[base + j];
+            }
+            ++o;
+        }
+    }
+}
+
+__device__ __forceinline__ int delta_at(const uint32_t* c, int i, int j, int n) {
+    return (j < 0 || j >= n) ? -1 : __clz((int)(c[i] ^ c[j]));
+}
+
+__global__ void __launch_bounds__(BUILD_THREADS)
+k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, const float4* __restrict__ tri_box,
+        const float4* __restrict__ tri_leaf, Node* nodes, float4* __restrict__ leaves, uint32_t* flags, int2* range,
+        BvhRoot* root, int* err) {
+    const int nt = root->n_tris;
+    const int n = min(root->n_leaves, nt);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t t = min(utri[i], (uint32_t)(nt - 1));
+    leaves[2 * i] = tri_leaf[2 * t];
+    leaves[2 * i + 1] = tri_leaf[2 * t + 1];
+    float4 lo = tri_box[2 * t], hi = tri_box[2 * t + 1];
+    if (n == 1) {
+        root->root = -1;
+        root->top_lo = lo;
+        root->top_hi = hi;
+        return;
+    }
+    int l = i, r = i;
+    int link = ~i;
+    // a leaf climbs at most 31 levels (distinct 30-bit codes); the bound only guards
+    // against a corrupted input after a failed look-back
+    for (int level = 0;; ++level) {
+        if (level > 64) {
+            atomicOr(err, ERR_TIMEOUT);
+            return;
+        }
+        const int dl = delta_at(ucode, l, l - 1, n);
+        const int dr = delta_at(ucode, r, r + 1, n);
+        int g;
+        if (dr > dl) {  // the parent extends to the right: this node is child A, split r
+            g = r;
+            nodes[g].a_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+            nodes[g].a_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
+            range[g].x = l;
+        } else {  // child B of the parent split at l - 1
+            g = l - 1;
+            nodes[g].b_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+            nodes[g].b_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
+            range[g].y = r;
+        }
+        __threadfence();
+        if (atomicAdd(&flags[g], 1u) == 0u) return;  // first child to arrive stops
+        __threadfence();
+        flags[g] = 0u;  // both children seen: ready for the next build
+        const int2 rg = __ldcg(&range[g]);
+        l = rg.x;
+        r = rg.y;
+        if (l < 0 || r >= n || l > r) {
+            atomicOr(err, ERR_TIMEOUT);
+            return;
+        }
+        const float4 alo = __ldcg(&nodes[g].a_lo), ahi = __ldcg(&nodes[g].a_hi);
+        const float4 blo = __ldcg(&nodes[g].b_lo), bhi = __ldcg(&nodes[g].b_hi);
+        // identity box (min +100, max -100) expanded by child A then child B
+        lo = make_float4(fminf(fminf(100.0f, alo.x), blo.x), fminf(fminf(100.0f, alo.y), blo.y),
+                         fminf(fminf(100.0f, alo.z), blo.z), 0.0f);
+        hi = make_float4(fmaxf(fmaxf(-100.0f, ahi.x), bhi.x), fmaxf(fmaxf(-100.0f, ahi.y), bhi.y),
+                         fmaxf(fmaxf(-100.0f, ahi.z), bhi.z), 0.0f);
+        link = g;
+        if (l == 0 && r == n - 1) {
+            root->root = g;
+            root->top_lo = lo;
+            root->top_hi = hi;
+            return;
+        }
+    }
+}
+
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
+    nv = nv_;
+    nt = nt_;
+    has_normals = normals;
+    tiles_sort = nt > 0 ? cdiv(nt, SORT_TILE) : 0;
+    int ni = nt > 1 ? nt - 1 : 1;
+    a.want(&xyz_in, (size_t)nv * 3 + 4);
+    a.want(&nrm_in, (size_t)nv * 3 + 4);
+    a.want(&verts, (size_t)nv + 1);
+    a.want(&tris, (size_t)nt * 3 + 4);
+    a.want(&tri_box, (size_t)nt * 2 + 2);
+    a.want(&tri_leaf, (size_t)nt * 2 + 2);
+    a.want(&codes, (size_t)nt + 1);
+    for (int k = 0; k < 2; ++k) {
+        a.want(&keys[k], (size_t)nt + 1);
+        a.want(&vals[k], (size_t)nt + 1);
+    }
+    a.want(&ucode, (size_t)nt + 1);
+    a.want(&utri, (size_t)nt + 1);
+    a.want(&nodes, (size_t)ni);
+    a.want(&leaves, (size_t)nt * 2 + 2);
+    a.want(&flags, (size_t)ni);
+    a.want(&range, (size_t)ni);
+    a.want(&root, 1);
+    // histograms | sort status (PASSES x tiles x RADIX) | sort counters | unique status | unique counter
+    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 1;
+    a.want(&scratch, scratch_words);
+}
+
+cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s) {
+    if (b.nt == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(b.scratch, 0, b.scratch_words * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    uint32_t* ghist = b.scratch;
+    uint32_t* sstat = ghist + PASSES * RADIX;
+    uint32_t* scount = sstat + (size_t)PASSES * b.tiles_sort * RADIX;
+    uint32_t* ustat = scount + PASSES;
+    uint32_t* ucount = ustat + b.tiles_sort;
+    k_body_prep<<<cdiv(b.nv, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.xyz_in, b.has_normals ? b.nrm_in : nullptr,
+                                                                     b.nv, thickness, b.verts, b.root, b.nt);
+    k_tri_boxes<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.verts, b.tris, b.nt, box_depth, b.tri_box,
+                                                                     b.tri_leaf, b.root);
+    k_morton<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.tri_box, b.nt, b.root, b.codes, ghist);
+    const uint32_t* kin = b.codes;
+    const uint32_t* vin = nullptr;
+    for (int p = 0; p < PASSES; ++p) {
+        uint32_t* ko = b.keys[p & 1];
+        uint32_t* vo = b.vals[p & 1];
+        k_sort_pass<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, ko, vo, b.nt, 8 * p, ghist + p * RADIX,
+                                                          sstat + (size_t)p * b.tiles_sort * RADIX, scount + p, d_err);
+        kin = ko;
+        vin = vo;
+    }
+    k_unique<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, b.nt, b.ucode, b.utri, ustat, ucount, b.tiles_sort,
+                                                   b.root, d_err);
+    k_build<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes,
+                                                                b.leaves, b.flags, b.range, b.root, d_err);
+    return cudaGetLastError();
+}
+
+}  // namespace visg

@@ -1,0 +1,336 @@
+// visg_step.cu — the fused cloth step and the first-hit query.
+//
+// k_step is the reference's `verlet` kernel (src/verlet.cu:129-161) rebuilt for
+// GB300: one thread per vertex, persistent CTAs walking a tile table (a tile is
+// BLOCK consecutive vertices of one garment, so one launch covers any number of
+// garments of uneven size), 32-byte interleaved state records read with two
+// float4 loads for the vertex and for every CSR neighbour, one merged CSR of
+// 8-byte entries with the list id in the top bits (no atomics), the previous
+// contact normal read only for vertices that had a contact, and the collision
+// (collision_response_projection, verlet.cu:24-50) fused behind a warp vote on the
+// body's root box.  Arithmetic follows the reference operation by operation with
+// explicit round-to-nearest intrinsics:
+//   v  = (x - xo) / dt
+//   F  = g*m + v*damp;  F += sum_list (sum_entry spring);  F -= (n_prev.F) n_prev
+//   spring = (-k (|d| - L0) + kd (dv.d)/|d|) * normalize(d),  d = x - x_j + FLT_EPSILON
+//   x' = (x + x - xo) + (F/m*dt)*dt       (gamma == 1, verlet.cu:155)
+//   x' = (x + gamma (x - xo)) + (F/m*dt)*dt  (damped Verlet)
+//   first-hit leaf (cudaBRT.cu:239-285) -> plane test (primitive.cu:110-125)
+//   -> x' += |dist| n, xo' = x', n_prev' = n; else n_prev' = 0
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "visg_internal.cuh"
+
+namespace visg {
+
+namespace {
+
+constexpr float kFltEpsilon = 1.1920928955078125e-07f;  // FLT_EPSILON
+constexpr int kStack = 32;  // > 30 = the depth bound of a radix tree over distinct 30-bit codes
+
+__device__ __forceinline__ bool in_box(f3 p, float4 lo, float4 hi) {  // BBox::intersect, inclusive
+    return (p.x >= lo.x && p.x <= hi.x) && (p.y >= lo.y && p.y <= hi.y) && (p.z >= lo.z && p.z <= hi.z);
+}
+
+// D_BVH::intersect semantics: children tested pairwise; an overlapping leaf child is
+// returned before any descent (A before B); both internal -> descend A, push B.
+// A depth-first walk visits every internal node at most once, so `budget` (the
+// number of internal nodes) bounds the loop even on a corrupted tree.
+__device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int node, int budget, f3 p, int* err) {
+    int stack[kStack];
+    int sp = 0;
+    while (true) {
+        if (--budget < 0) {
+            atomicOr(err, ERR_STACK);
+            return -1;
+        }
+        const Node* nd = nodes + node;
+        const float4 alo = __ldg(&nd->a_lo), ahi = __ldg(&nd->a_hi);
+        const float4 blo = __ldg(&nd->b_lo), bhi = __ldg(&nd->b_hi);
+        const int la = __float_as_int(alo.w), lb = __float_as_int(blo.w);
+        const bool ol = in_box(p, alo, ahi), orr = in_box(p, blo, bhi);
+        if (ol && la < 0) return ~la;
+        if (orr && lb < 0) return ~lb;
+        const bool tl = ol && la >= 0, tr = orr && lb >= 0;
+        if (!tl && !tr) {
+            if (sp == 0) return -1;
+            node = stack[--sp];
+        } else {
+            node = tl ? la : lb;
+            if (tl && tr) {
+                if (sp == kStack) {
+                    atomicOr(err, ERR_STACK);
+                    return -1;
+                }
+                stack[sp++] = lb;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ int query_leaf(const BvhView& bv, int n_leaves, int root, float4 top_lo, float4 top_hi,
+                                          f3 p, int* err) {
+    if (n_leaves <= 0 || !in_box(p, top_lo, top_hi)) return -1;
+    if (n_leaves == 1) return 0;
+    return first_hit(bv.nodes, root, n_leaves, p, err);
+}
+
+template <int BLOCK, bool PERK, bool COLL>
+__global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check) {
+    const StepParams& P = a.p;
+    const f3 grav = mk3(P.gx, P.gy, P.gz);
+    const f3 eps3 = mk3(kFltEpsilon, kFltEpsilon, kFltEpsilon);
+    float my_disp = 0.0f;
+    uint32_t my_bad = 0;
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const int4 td = __ldg(&a.tiles[tile]);
+        const int i = td.y + (int)threadIdx.x;
+        const bool active = i < td.z;
+        const int ii = active ? i : td.y;
+        const float4 s0 = __ldg(&a.state_in[2 * ii]);
+        const float4 s1 = __ldg(&a.state_in[2 * ii + 1]);
+        const f3 x = mk3(s0.x, s0.y, s0.z);
+        const f3 xo = mk3(s0.w, s1.x, s1.y);
+        const uint32_t flags = __float_as_uint(s1.z);
+        uint32_t rp = __ldg(&a.rowp[ii]);
+        const uint32_t re = __ldg(&a.rowp[ii + 1]) & ROW_MASK;
+        const bool pinned = (rp & PIN_BIT) != 0u;
+        rp &= ROW_MASK;
+        f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
+        bool has_n = false;
+        if (!pinned) {
+            f3 np = mk3(0.0f, 0.0f, 0.0f);
+            if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
+            const f3 vel = divs(sub(x, xo), P.dt);
+            f3 F = add(mul(grav, P.mass), mul(vel, P.damp));
+            f3 acc = mk3(0.0f, 0.0f, 0.0f);
+            int list = 0;
+            for (uint32_t e = rp; e < re; ++e) {
+                const uint2 en = __ldg(&a.ent[e]);
+                const int j = (int)(en.x & END_MASK);
+                const int f = (int)(en.x >> LIST_SHIFT);
+                while (list < f) {  // list boundary: force += that list's sum (verlet.cu:148-149)
+                    F = add(F, acc);
+                    acc = mk3(0.0f, 0.0f, 0.0f);
+                    ++list;
+                }
+                const float ks = PERK ? __ldg(&a.kent[e]) : P.list_k[f];
+                const float4 t0 = __ldg(&a.state_in[2 * j]);
+                const float4 t1 = __ldg(&a.state_in[2 * j + 1]);
+                const f3 p2 = mk3(t0.x, t0.y, t0.z);
+                const f3 p2o = mk3(t0.w, t1.x, t1.y);
+                const f3 v2 = divs(sub(p2, p2o), P.dt);
+                const f3 dP = add(sub(x, p2), eps3);
+                const f3 dV = sub(vel, v2);
+                const float dist = length(dP);
+                const float left = __fmul_rn(-ks, __fsub_rn(dist, __uint_as_float(en.y)));
+                const float right = __fmul_rn(P.kd, __fdiv_rn(dot(dV, dP), dist));
+                acc = add(acc, mul(__fadd_rn(left, right), normalize(dP)));
+            }
+            while (list < P.n_lists) {
+                F = add(F, acc);
+                acc = mk3(0.0f, 0.0f, 0.0f);
+                ++list;
+            }
+            F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
+            const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
+            if (refv) xn = add(sub(add(x, x), xo), adt);
+            else xn = add(add(x, mul(P.gamma, sub(x, xo))), adt);
+            xon = x;
+        }
+        if (COLL) {
+            const BvhView bv = a.bodies[td.x];
+            if (bv.root != nullptr) {
+                const int nl = bv.root->n_leaves;
+                const int rt = bv.root->root;
+                const float4 tlo = bv.root->top_lo, thi = bv.root->top_hi;
+                const bool cand = active && !pinned && nl > 0 && in_box(xn, tlo, thi);
+                if (__any_sync(0xffffffffu, cand)) {
+                    if (cand) {
+                        const int leaf = nl == 1 ? 0 : first_hit(bv.nodes, rt, nl, xn, a.err);
+                        if (leaf >= 0) {
+                            const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
+                            const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
+                            const f3 n = mk3(L0.w, L1.x, L1.y);
+                            const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), n);
+                            if (!(d > 0.0f)) {
+                                xn = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), n));
+                                xon = xn;
+                                nn = n;
+                                has_n = true;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (active) {
+            a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, xon.x);
+            a.state_out[2 * i + 1] = make_float4(xon.y, xon.z, __uint_as_float(has_n ? FLAG_HAS_NORMAL : 0u), 0.0f);
+            if (has_n) a.normal[i] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+            if (check) {
+                const float dd = fmaxf(fabsf(__fsub_rn(xn.x, x.x)), fmaxf(fabsf(__fsub_rn(xn.y, x.y)), fabsf(__fsub_rn(xn.z, x.z))));
+                if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(xon.x) || !isfinite(xon.y) ||
+                    !isfinite(xon.z))
+                    ++my_bad;
+                else
+                    my_disp = fmaxf(my_disp, dd);
+            }
+        }
+    }
+    if (check) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            my_disp = fmaxf(my_disp, __shfl_xor_sync(0xffffffffu, my_disp, o));
+            my_bad += __shfl_xor_sync(0xffffffffu, my_bad, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (my_disp > 0.0f) atomicMax(&a.check[0], __float_as_uint(my_disp));
+            if (my_bad) atomicAdd(&a.check[1], my_bad);
+        }
+    }
+}
+
+template <int BLOCK>
+cudaError_t launch_block(const StepArgs& a, int variant, int grid, cudaStream_t s) {
+    const int refv = (variant & SV_REFV) ? 1 : 0;
+    const int check = (variant & SV_CHECK) ? 1 : 0;
+    const bool perk = (variant & SV_PERK) != 0, coll = (variant & SV_COLLIDE) != 0;
+    if (perk && coll) k_step<BLOCK, true, true><<<grid, BLOCK, 0, s>>>(a, refv, check);
+    else if (perk) k_step<BLOCK, true, false><<<grid, BLOCK, 0, s>>>(a, refv, check);
+    else if (coll) k_step<BLOCK, false, true><<<grid, BLOCK, 0, s>>>(a, refv, check);
+    else k_step<BLOCK, false, false><<<grid, BLOCK, 0, s>>>(a, refv, check);
+    return cudaGetLastError();
+}
+
+template <int BLOCK>
+int occupancy_block(int variant) {
+    int n = 0;
+    const bool perk = (variant & SV_PERK) != 0, coll = (variant & SV_COLLIDE) != 0;
+    if (perk && coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, true>, BLOCK, 0);
+    else if (perk) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, false>, BLOCK, 0);
+    else if (coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, true>, BLOCK, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, false>, BLOCK, 0);
+    return n;
+}
+
+__global__ void k_query(BvhView bv, const float* __restrict__ pts, int n, int* leaf, int* inside, float* dist,
+                        float* normal, int* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f3 p = mk3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+    const int nl = bv.root->n_leaves;
+    const int lf = query_leaf(bv, nl, bv.root->root, bv.root->top_lo, bv.root->top_hi, p, err);
+    float d = 0.0f;
+    f3 nn = mk3(0.0f, 0.0f, 0.0f);
+    int in = 0;
+    if (lf >= 0) {
+        const float4 L0 = bv.leaves[2 * lf], L1 = bv.leaves[2 * lf + 1];
+        nn = mk3(L0.w, L1.x, L1.y);
+        d = dot(sub(p, mk3(L0.x, L0.y, L0.z)), nn);
+        in = !(d > 0.0f);
+    }
+    if (leaf) leaf[i] = lf;
+    if (inside) inside[i] = in;
+    if (dist) dist[i] = d;
+    if (normal) {
+        normal[3 * i] = nn.x;
+        normal[3 * i + 1] = nn.y;
+        normal[3 * i + 2] = nn.z;
+    }
+}
+
+__global__ void k_unpack_positions(const float4* __restrict__ st, int64_t n, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 s0 = st[2 * i];
+    out[3 * i] = s0.x;
+    out[3 * i + 1] = s0.y;
+    out[3 * i + 2] = s0.z;
+}
+
+__global__ void k_unpack_state(const float4* __restrict__ st, const float4* __restrict__ nr, int64_t n, float* x,
+                               float* xo, float* nrm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 s0 = st[2 * i], s1 = st[2 * i + 1];
+    if (x) { x[3 * i] = s0.x; x[3 * i + 1] = s0.y; x[3 * i + 2] = s0.z; }
+    if (xo) { xo[3 * i] = s0.w; xo[3 * i + 1] = s1.x; xo[3 * i + 2] = s1.y; }
+    if (nrm) {
+        const bool h = (__float_as_uint(s1.z) & FLAG_HAS_NORMAL) != 0u;
+        const float4 v = h ? nr[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        nrm[3 * i] = v.x; nrm[3 * i + 1] = v.y; nrm[3 * i + 2] = v.z;
+    }
+}
+
+// x == nullptr keeps x, etc.  A vertex has a stored normal iff it is non-zero.
+__global__ void k_pack_state(float4* st, float4* nr, int64_t n, const float* x, const float* xo, const float* nrm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 s0 = st[2 * i], s1 = st[2 * i + 1];
+    if (x) { s0.x = x[3 * i]; s0.y = x[3 * i + 1]; s0.z = x[3 * i + 2]; }
+    if (xo) { s0.w = xo[3 * i]; s1.x = xo[3 * i + 1]; s1.y = xo[3 * i + 2]; }
+    if (nrm) {
+        const float a = nrm[3 * i], b = nrm[3 * i + 1], c = nrm[3 * i + 2];
+        const bool h = a != 0.0f || b != 0.0f || c != 0.0f;
+        nr[i] = make_float4(a, b, c, 0.0f);
+        s1.z = __uint_as_float(h ? FLAG_HAS_NORMAL : 0u);
+    }
+    s1.w = 0.0f;
+    st[2 * i] = s0;
+    st[2 * i + 1] = s1;
+}
+
+inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s) {
+    if (a.n_tiles == 0) return cudaSuccess;
+    if (grid <= 0 || grid > a.n_tiles) grid = a.n_tiles;
+    switch (block) {
+        case 128: return launch_block<128>(a, variant, grid, s);
+        case 256: return launch_block<256>(a, variant, grid, s);
+        case 512: return launch_block<512>(a, variant, grid, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+int step_max_ctas_per_sm(int variant, int block) {
+    switch (block) {
+        case 128: return occupancy_block<128>(variant);
+        case 256: return occupancy_block<256>(variant);
+        case 512: return occupancy_block<512>(variant);
+        default: return 0;
+    }
+}
+
+cudaError_t launch_query(BvhView v, const float* pts, int n, int* leaf, int* inside, float* dist, float* normal,
+                         int* err, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_query<<<grid_for(n, 256), 256, 0, s>>>(v, pts, n, leaf, inside, dist, normal, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_positions(const float4* state, int64_t n, float* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_unpack_positions<<<grid_for(n, 256), 256, 0, s>>>(state, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_state(const float4* state, const float4* normal, int64_t n, float* x, float* xo, float* nrm,
+                                cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_unpack_state<<<grid_for(n, 256), 256, 0, s>>>(state, normal, n, x, xo, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_state(float4* state, float4* normal, int64_t n, const float* x, const float* xo,
+                              const float* nrm, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, normal, n, x, xo, nrm);
+    return cudaGetLastError();
+}
+
+}  // namespace visg

@@ -1,0 +1,325 @@
+"""GPU parity: the CUDA library through its C ABI against the oracle (CPU
+restatement, float and FP64) and against the reference's own kernels (refkern).
+
+Bars: integers (Morton codes, sorted order, tree links, first-hit leaves)
+bit-exact; LBVH boxes exactly equal; positions, previous positions and contact
+normals of single steps and of trajectories bit-exact against the float oracle
+(the library and the oracle perform the same IEEE operations in the same order)
+and within 1e-6 relative per step / 1e-4 m per trajectory of the FP64 oracle
+where the FP64 comparison is meaningful.
+"""
+import numpy as np
+import pytest
+
+import simulator_gb300 as vs
+from helpers import config_params, lbvh_diff, ref_scene, soup
+from oracle import ffi
+from oracle.ffi import OracleSim
+from simulator_gb300 import scenes
+from simulator_gb300.params import reference_params
+
+pytestmark = pytest.mark.gpu
+
+TRAJ_TOL = 1e-4  # metres, 200-step trajectory vs FP64
+STEP_REL = 1e-6  # single step vs FP64, relative to the displacement scale
+
+
+def lbvh_pair(xyz, tris, normals=None, thickness=0.003):
+    cloth = scenes.grid_cloth(4, 1.0, 5.0, pin_top_corners=False)
+    p = reference_params(3)
+    p.thickness = thickness
+    g = vs.Simulator(cloth.xyz, cloth.lists, xyz, tris, normals, params=p)
+    o = OracleSim(p, cloth.xyz, cloth.lists, xyz, tris, normals, prec=4)
+    return g, o
+
+
+BODIES = {
+    "ico0": lambda: scenes.icosphere(0, 0.3),
+    "ico3_noise": lambda: scenes.icosphere(3, 0.3, (0.1, -0.5, 0.2), noise=0.02, seed=3),
+    "ico5_noise": lambda: scenes.icosphere(5, 0.3, (0.0, -0.5, 0.0), noise=0.02, seed=5),
+    "ico6": lambda: scenes.icosphere(6, 0.4, (0.0, -0.5, 0.0)),
+    "capsules": lambda: scenes.three_capsules(),
+}
+
+
+@pytest.mark.parametrize("name", list(BODIES))
+def test_lbvh_bodies_match_oracle(name):
+    b = BODIES[name]()
+    g, o = lbvh_pair(b.xyz, b.tris, b.normals)
+    a, r = g.export_lbvh(), o.export_lbvh()
+    assert lbvh_diff(a, r) == []
+
+
+@pytest.mark.parametrize("n,dup", [(1, 0.0), (2, 0.0), (3, 0.0), (127, 0.0), (128, 0.0), (129, 0.0),
+                                   (2047, 0.2), (2048, 0.2), (2049, 0.2), (4096, 0.5), (100003, 0.3)])
+def test_lbvh_soups_match_oracle(n, dup):
+    xyz, tris = soup(n, seed=n, dup_frac=dup)
+    g, o = lbvh_pair(xyz, tris)
+    assert lbvh_diff(g.export_lbvh(), o.export_lbvh()) == []
+
+
+def test_lbvh_single_distinct_code():
+    one = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    xyz = np.concatenate([one] * 7)
+    tris = np.arange(21, dtype=np.uint32).reshape(7, 3)
+    g, o = lbvh_pair(xyz, tris)
+    a, r = g.export_lbvh(), o.export_lbvh()
+    assert a["n_leaves"] == 1 and lbvh_diff(a, r) == []
+    pts = np.array([[0.2, 0.2, -0.005], [0.2, 0.2, 0.5], [5, 5, 5]], np.float32)
+    ga, oa = g.query(pts), o.query(pts)
+    assert np.array_equal(ga[0], oa[0]) and np.array_equal(ga[1], oa[1])
+
+
+def test_lbvh_rebuild_after_update_matches_oracle():
+    b = scenes.icosphere(4, 0.3, (0.0, -0.5, 0.0), noise=0.02, seed=1)
+    g, o = lbvh_pair(b.xyz, b.tris, b.normals)
+    for k in range(3):
+        moved = scenes.translated(b, (0.01 * k, -0.05 * k, 0.02 * k))
+        g.update_body(moved, b.normals)
+        o.update_body(moved, b.normals)
+        assert lbvh_diff(g.export_lbvh(), o.export_lbvh()) == []
+
+
+@pytest.mark.parametrize("name", ["ico3_noise", "capsules"])
+def test_first_hit_queries_match_oracle(name):
+    b = BODIES[name]()
+    g, o = lbvh_pair(b.xyz, b.tris, b.normals)
+    rng = np.random.default_rng(7)
+    lo, hi = b.xyz.min(0) - 0.02, b.xyz.max(0) + 0.02
+    pts = rng.uniform(lo, hi, size=(20000, 3)).astype(np.float32)
+    gl, gi, gd, gn = g.query(pts)
+    ol, oi, od, on = o.query(pts)
+    assert np.array_equal(gl, ol)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gd, od.astype(np.float32))
+    assert np.array_equal(gn, on.astype(np.float32))
+    assert gi.sum() > 100
+
+
+def run_pair(cloth, lists, body, p, steps, pinned=None, moving=None):
+    g = vs.Simulator(cloth.xyz, lists, body.xyz if body else None, body.tris if body else None,
+                     body.normals if body else None, params=p, pinned=pinned)
+    o = OracleSim(p, cloth.xyz, lists, body.xyz if body else None, body.tris if body else None,
+                  body.normals if body else None, prec=4, pinned=pinned)
+    for k in range(steps):
+        if moving is not None:
+            xyz = moving(k)
+            g.update_body(xyz, body.normals)
+            o.update_body(xyz, body.normals)
+        g.simulate(1)
+        o.step(1)
+    return g, o
+
+
+def assert_state_equal(g, o, mask=None):
+    x, xo, n = g.state()
+    ox, oxo, on = o.state()
+    sl = slice(None) if mask is None else mask
+    assert np.array_equal(x[sl], ox.astype(np.float32)[sl]), np.abs(x - ox)[sl].max()
+    assert np.array_equal(xo[sl], oxo.astype(np.float32)[sl])
+    assert np.array_equal(n[sl], on.astype(np.float32)[sl])
+    return x, n
+
+
+@pytest.mark.parametrize("lists", ["grid", "mesh"])
+def test_steps_bitexact_vs_float_oracle(lists):
+    cloth, cl, body, p = ref_scene(side=32, subdiv=3, lists=lists)
+    g, o = run_pair(cloth, cl, body, p, 1)
+    assert_state_equal(g, o)
+    g.simulate(79)
+    o.step(79)
+    x, n = assert_state_equal(g, o)
+    assert (np.abs(n).sum(1) > 0).sum() > 10, "the sheet must be in contact"
+
+
+def test_config_physics_pinned_vs_oracle():
+    cloth = scenes.grid_cloth(40, 1.0, 0.0)
+    body = scenes.icosphere(4, 0.3, (0.0, -0.32, 0.0))
+    p = config_params(substeps=2)
+    g, o = run_pair(cloth, cloth.lists, body, p, 1, pinned=cloth.pinned)
+    g.simulate(299)
+    o.step(299)
+    x, n = assert_state_equal(g, o)
+    assert np.array_equal(x[cloth.pinned], cloth.xyz[cloth.pinned])
+    assert (np.abs(n).sum(1) > 0).sum() > 10
+
+
+def test_moving_body_rebuilt_every_step_vs_oracle():
+    cloth = scenes.grid_cloth(28, 1.0, 0.0, jitter=1e-4, seed=3, pin_top_corners=False)
+    body = scenes.three_capsules(center=(0.0, -0.35, 0.0))
+    p = reference_params(3)
+    p.list_k[:] = (100.0, 60.0, 2.0, 0.0)
+    g, o = run_pair(cloth, cloth.lists, body, p, 60, moving=lambda k: scenes.translated(body, (0, 0.002 * k, 0)))
+    x, n = assert_state_equal(g, o)
+    assert (np.abs(n).sum(1) > 0).sum() > 5
+
+
+def test_trajectory_vs_fp64():
+    cloth, cl, body, p = ref_scene(side=32, subdiv=3)
+    g = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    o = OracleSim(p, cloth.xyz, cl, body.xyz, body.tris, body.normals, prec=8)
+    x0 = cloth.xyz.astype(np.float64)
+    g.simulate(1)
+    o.step(1)
+    x1, _, _ = g.state()
+    ox1, _, _ = o.state()
+    scale = np.abs(ox1 - x0).max()
+    assert np.abs(x1 - ox1).max() <= STEP_REL * max(scale, np.abs(ox1).max())
+    g.simulate(199)
+    o.step(199)
+    x, _, _ = g.state()
+    ox, _, _ = o.state()
+    err = np.abs(x - ox).max()
+    print(f"200-step max |x_f32 - x_f64| = {err:.3e} m")
+    assert err <= TRAJ_TOL
+
+
+def test_graph_replay_equals_single_launches():
+    cloth, cl, body, p = ref_scene(side=20, subdiv=2)
+    p1 = reference_params(3)
+    p1.list_k[:] = p.list_k[:]
+    p1.use_graph = 0
+    a = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    b = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p1)
+    a.simulate(37)
+    b.simulate(37)
+    for u, v in zip(a.state(), b.state()):
+        assert np.array_equal(u, v)
+
+
+def test_set_vertex_and_state_roundtrip():
+    cloth, cl, body, p = ref_scene(side=16, subdiv=2)
+    g = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    o = OracleSim(p, cloth.xyz, cl, body.xyz, body.tris, body.normals, prec=4)
+    g.simulate(40)
+    o.step(40)
+    g.update_vertex([0.1, 0.2, 0.3], 5)
+    o.set_vertex(5, [0.1, 0.2, 0.3])
+    g.simulate(3)
+    o.step(3)
+    assert_state_equal(g, o)
+    x, xo, n = g.state()
+    g2 = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    g2.set_state(x, xo, n)
+    g.simulate(5)
+    g2.simulate(5)
+    for u, v in zip(g.state(), g2.state()):
+        assert np.array_equal(u, v)
+    assert np.array_equal(g.positions(), g.state()[0])
+
+
+def test_batch_equals_plain_per_garment():
+    p = reference_params(3)
+    p.list_k[:] = (100.0, 60.0, 2.0, 0.0)
+    rng = np.random.default_rng(11)
+    items = []
+    for k in range(5):
+        side = int(rng.integers(5, 40))
+        cloth = scenes.grid_cloth(side, 1.0, 0.0, pin_top_corners=bool(k % 2))
+        body = scenes.icosphere(int(rng.integers(1, 4)), 0.25, (0.0, -0.3, 0.0))
+        items.append((cloth, body))
+    items.append((scenes.grid_cloth(9, 1.0, 0.0), None))  # a garment without a body
+    b = vs.BatchSimulator(p)
+    for cloth, body in items:
+        b.add(cloth.xyz, cloth.lists, None if body is None else body.xyz, None if body is None else body.tris,
+              None if body is None else body.normals, pinned=cloth.pinned)
+    b.finalize()
+    b.step(45)
+    allx = b.positions()
+    for gi, (cloth, body) in enumerate(items):
+        s = vs.Simulator(cloth.xyz, cloth.lists, None if body is None else body.xyz,
+                         None if body is None else body.tris, None if body is None else body.normals, params=p,
+                         pinned=cloth.pinned)
+        s.simulate(45)
+        x = s.positions()
+        assert np.array_equal(b.positions(gi), x)
+        assert np.array_equal(allx[b.offsets[gi]:b.offsets[gi + 1]], x)
+
+
+def test_batch_autotune_keeps_state_and_results():
+    p = reference_params(3)
+    items = [(scenes.grid_cloth(s, 1.0, 0.0), scenes.icosphere(2, 0.3, (0, -0.3, 0))) for s in (30, 50, 70)]
+    a, c = vs.BatchSimulator(p), vs.BatchSimulator(p)
+    for cloth, body in items:
+        for bb in (a, c):
+            bb.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+    a.finalize()
+    c.finalize()
+    a.step(10)
+    c.step(10)
+    blk, ctas = a.autotune()
+    assert blk in (128, 256, 512)
+    a.step(30)
+    c.step(30)
+    assert np.array_equal(a.positions(), c.positions())
+
+
+def test_divergence_reported():
+    cloth = scenes.grid_cloth(16, 1.0, 0.0)
+    p = config_params(substeps=1)  # one step per 1e-3 s frame: unstable
+    p.check_every = 50
+    p.max_displacement = 0.05
+    g = vs.Simulator(cloth.xyz, cloth.lists, params=p, pinned=cloth.pinned)
+    with pytest.raises(vs.VisgError) as e:
+        g.simulate(400)
+    assert e.value.code == -5
+
+
+def test_invalid_arguments_rejected():
+    cloth = scenes.grid_cloth(6)
+    p = reference_params(3)
+    bad = [scenes.SpringList(sl.row.copy(), sl.ent.copy()) for sl in cloth.lists]
+    bad[0].ent["end"][3] = 10_000
+    with pytest.raises(vs.VisgError) as e:
+        vs.Simulator(cloth.xyz, bad, params=p)
+    assert e.value.code == -1
+    g = vs.Simulator(cloth.xyz, cloth.lists, params=p)
+    with pytest.raises(vs.VisgError):
+        g.set_pinned([36])
+    with pytest.raises(vs.VisgError):
+        g.update_vertex([0, 0, 0], 36)
+    with pytest.raises(vs.VisgError):
+        g.update_body(np.zeros((3, 3), np.float32))  # no body at creation
+
+
+# ---------------------------------------------------------------------------------------
+# against the reference's own kernels
+# ---------------------------------------------------------------------------------------
+needs_ref = pytest.mark.skipif(not ffi.refkern_available(), reason="refkern cubin not built")
+
+
+@needs_ref
+@pytest.mark.parametrize("name", ["ico3_noise", "ico5_noise", "capsules"])
+def test_lbvh_matches_reference_kernels(name):
+    b = BODIES[name]()
+    cloth, cl, _, p = ref_scene(side=8, lists="mesh")
+    r = ffi.RefSim(p, cloth.xyz, cl, b.xyz, b.tris, b.normals)
+    g = vs.Simulator(cloth.xyz, cl, b.xyz, b.tris, b.normals, params=p)
+    assert lbvh_diff(g.export_lbvh(), r.export_lbvh()) == []
+
+
+@needs_ref
+def test_lbvh_soup_with_duplicates_matches_reference_kernels():
+    xyz, tris = soup(5000, seed=9, dup_frac=0.4)
+    cloth, cl, _, p = ref_scene(side=8, lists="mesh")
+    r = ffi.RefSim(p, cloth.xyz, cl, xyz, tris)
+    g = vs.Simulator(cloth.xyz, cl, xyz, tris, params=p)
+    assert lbvh_diff(g.export_lbvh(), r.export_lbvh()) == []
+
+
+@needs_ref
+def test_trajectory_matches_reference_kernels():
+    cloth, cl, body, p = ref_scene(side=32, subdiv=3, lists="mesh")
+    r = ffi.RefSim(p, cloth.xyz, cl, body.xyz, body.tris, body.normals)
+    g = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    g.simulate(1)
+    r.step(1)
+    for u, v in zip(g.state(), r.state()):
+        assert np.array_equal(u, v)
+    g.simulate(199)
+    r.step(199)
+    x, xo, n = g.state()
+    rx, rxo, rn = r.state()
+    print(f"200 steps vs reference kernels: max |dx| = {np.abs(x - rx).max():.3e}")
+    assert np.abs(x - rx).max() <= TRAJ_TOL
+    assert (np.abs(rn).sum(1) > 0).sum() > 10
