@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 cloth step: cloth vertex-steps/s.
+
+Default workload (the one the metric "batched vs plain" is quoted on): 256
+garments in one batch, garment side ~ U{32..256} vertices (a 1 m sheet with the
+structural / shear / bend spring lists, k = 2000 / 1000 / 500), each facing its own
+icosphere (subdivision ~ U{3..6}, radius ~ U[0.2, 0.4] m), seeded synthetic data.
+A "step" is one pass of the fused step kernel over every garment (integrate +
+springs + first-hit collision); the physics uses 2 steps per 1e-3 s frame (one
+step per frame is linearly unstable at these stiffnesses).
+
+Reported (one JSON line, rank 0):
+  value       batched vertex-steps/s, device-resident inputs, CUDA events on the
+              launching stream around K steps (graph replay), max over ranks
+  e2e         the same through the C ABI with host buffers: every step uploads the
+              pinned-vertex targets from pinned host memory, steps, and reads all
+              positions back into pinned host memory
+  plain_loop  the same garments as 256 plain simulators stepped one after another
+  roofline    the fused step kernel: algorithmic bytes per launch / launch time
+  cpu_baseline the CPU restatement (OpenMP) on the same garments, bounded sample
+`--impl reference` times the reference's step logic on the host cores (the
+oracle port; the reference itself is CUDA only) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "fused_step_batched256.md")
+METRIC = "cloth vertex-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--garments", type=int, default=256)
+    ap.add_argument("--substeps", type=int, default=2)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-garment loop")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-autotune", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------
+def build_workload(n_garments: int, seed: int):
+    from simulator_gb300 import scenes
+    items = scenes.garment_batch(n_garments, seed=seed)
+    nv = sum(len(c.xyz) for c, _ in items)
+    ne = sum(sum(sl.n_entries for sl in c.lists) for c, _ in items)
+    nt = sum(len(b.tris) for _, b in items)
+    return items, nv, ne, nt
+
+
+def workload_name(args):
+    return (f"batched: {args.garments} garments, side ~ U{{32..256}} (1 m sheet, structural/shear/bend lists), "
+            f"own icosphere subdiv ~ U{{3..6}}, r ~ U[0.2,0.4] m; {args.substeps} steps per 1e-3 s frame")
+
+
+def peak_hbm():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+def committed_traffic():
+    """Per-launch DRAM bytes of the fused step from the committed ncu summary."""
+    try:
+        text = open(TRAFFIC_FILE).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        rows = []
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                rows.append(dict(sm=float(f[1]), smax=float(f[2]), util=float(f[4]), hw=f[6], hwt=f[7], swt=f[8],
+                                 pcap=f[9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        load = [r for r in rows if r["util"] >= 50.0] or rows
+        reasons = set()
+        for r in load:
+            if r["hw"] == "Active":
+                reasons.add("hw_slowdown")
+            if r["hwt"] == "Active":
+                reasons.add("hw_thermal_slowdown")
+            if r["swt"] == "Active":
+                reasons.add("sw_thermal_slowdown")
+            if r["pcap"] == "Active":
+                reasons.add("sw_power_cap")
+        return {"sm_mhz": statistics.median(r["sm"] for r in load), "sm_max_mhz": max(r["smax"] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows), "samples_under_load": len(load)}
+
+
+def cpu_baseline(items, params, seconds: float):
+    """The oracle (the reference's step restated in C++, float, OpenMP over the
+    vertices of each garment) stepping the same garments; bounded sample."""
+    from oracle.ffi import OracleSim, num_threads
+    threads = num_threads(0)
+    sims = [OracleSim(params, c.xyz, c.lists, b.xyz, b.tris, b.normals, prec=4, pinned=c.pinned) for c, b in items]
+    nv = sum(s.n for s in sims)
+    for s in sims:  # one untimed step
+        s.step(1)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        for s in sims:
+            s.step(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 1000:
+            break
+    for s in sims:
+        s.close()
+    return {"value": nv * steps / el, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
+            "sample": f"all {len(items)} garments ({nv} vertices) for {steps} steps ({el:.1f} s), "
+                      f"{threads} OpenMP threads"}
+
+
+# ---------------------------------------------------------------------------------------
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    from simulator_gb300 import scenes
+    items, nv, ne, nt = build_workload(args.garments, args.seed)
+    params = scenes.physics_params(args.substeps)
+    base = cpu_baseline(items, params, args.cpu_seconds)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "vertex-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(args), "garments": args.garments, "vertices": nv,
+                   "spring_entries": ne, "triangles": nt},
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    import simulator_gb300 as vs
+    from simulator_gb300 import scenes
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    phys = int(vis.split(",")[local]) if vis and vis.split(",")[local].strip().isdigit() else local
+    sampler = ClockSampler(phys)
+
+    params = scenes.physics_params(args.substeps)
+    items, nv, ne, nt = build_workload(args.garments, args.seed + rank)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    b = vs.BatchSimulator(params)
+    pins = []
+    off = 0
+    for cloth, body in items:
+        b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+        pins.append(cloth.pinned.astype(np.int64) + off)
+        off += len(cloth.xyz)
+    b.finalize()
+    b.set_stream(sh)
+    pins = np.concatenate(pins).astype(np.uint32)
+    pin_xyz0 = np.concatenate([c.xyz[c.pinned] for c, _ in items]).astype(np.float32)
+    blk, ctas = (256, 0) if args.no_autotune else b.autotune()
+
+    sampler.start()
+    # ---- device-resident value: K steps replayed from CUDA graphs --------------------
+    b.step(args.warmup)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    value = world * nv * args.steps / (ms / 1e3)
+    contacts = b.count_contacts()
+
+    # ---- end to end through the C ABI with host buffers --------------------------------
+    host_out = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
+    out_np = host_out.numpy()
+    pin_host = torch.empty((len(pins), 3), dtype=torch.float32, pin_memory=True).numpy()
+    k_e2e = max(1, min(args.steps, 50))
+    for k in range(2):  # warm the staging buffers
+        b.update_vertices(pins, pin_xyz0)
+        b.step(1)
+        b.positions(out=out_np)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(k_e2e):
+        pin_host[:] = pin_xyz0  # the step's host input: pinned-vertex targets
+        b.update_vertices(pins, pin_host)
+        b.step(1)
+        b.positions(out=out_np)  # the step's result back in host memory (synchronises)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * nv * k_e2e / e2e_s
+    h2d = len(pins) * (4 + 12)
+    d2h = nv * 12
+
+    # ---- the plain per-garment loop on the same GPU ------------------------------------
+    plain = None
+    if not args.no_plain:
+        sims = []
+        for cloth, body in items:
+            s = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
+                             pinned=cloth.pinned)
+            s.set_stream(sh)
+            sims.append(s)
+        for s in sims:
+            s.simulate(args.warmup)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for s in sims:
+            s.simulate(args.steps)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = max_over_ranks(p0.elapsed_time(p1))
+        plain = {"value": world * nv * args.steps / (pms / 1e3), "ms_per_step": pms / args.steps,
+                 "how": "each garment its own Simulator, stepped K steps (graph replay) one garment after another"}
+        for s in sims:
+            s.close()
+    clocks = sampler.stop()
+
+    # ---- roofline of the fused step kernel ---------------------------------------------
+    alg_bytes = 64 * nv + 4 * (nv + 1) + 8 * ne + 32 * contacts
+    t_launch = ms / 1e3 / args.steps
+    achieved = alg_bytes / t_launch / 1e9
+    peak, peak_kind = peak_hbm()
+    traffic = committed_traffic()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(items, params, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": workload_name(args), "garments": args.garments, "vertices_per_gpu": nv,
+                       "spring_entries": ne, "triangles": nt, "contacts": contacts,
+                       "launch": {"block": blk, "ctas_per_sm": ctas},
+                       "l2": f"inputs larger than L2: {alg_bytes / 1e6:.0f} MB moved per step vs 129 MB L2",
+                       "parallelism": f"{world} independent batches (one per GPU)"},
+            "e2e": {"value": e2e_value, "unit": "vertex-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": k_e2e},
+            "plain_loop": plain,
+            "batched_vs_plain": (value / plain["value"]) if plain else None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_step (fused integrate + springs + collision)",
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -118,6 +118,11 @@ int visg_update_body_device(VisgSim* sim, const float* d_body_xyz, const float* 
  * one vertex (its velocity becomes zero). */
 int visg_set_vertex(VisgSim* sim, uint32_t idx, const float xyz[3]);
 
+/* update_vertex for many vertices in one call: idx[k] gets x = x_old = xyz[3k..3k+2].
+ * One host-to-device copy and one scatter kernel, asynchronous on the stream (the
+ * host arrays are staged before the call returns).  Duplicate indices: the last wins. */
+int visg_set_vertices(VisgSim* sim, const uint32_t* idx, const float* xyz, int32_t n);
+
 /* Pinned vertices keep x and get x_old = x every step (the reference's drag via
  * update_vertex called before every step). n == 0 clears all pins. */
 int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n);
@@ -136,6 +141,9 @@ int visg_set_state(VisgSim* sim, const float* x, const float* x_old, const float
 /* Waits for the stream; returns the first device-side error recorded since the
  * last call (VISG_ERR_DIVERGED, VISG_ERR_TIMEOUT) or VISG_OK. */
 int visg_sync(VisgSim* sim);
+
+/* Number of vertices whose last step ended in contact (stored normal non-zero). Synchronises. */
+int visg_count_contacts(VisgSim* sim, int64_t* n);
 
 int visg_get_info(VisgSim* sim, int32_t* n_vertices, int32_t* n_entries,
                   int32_t* n_tris, int32_t* n_leaves);
@@ -201,6 +209,9 @@ int visg_batch_step(VisgBatch* b, int32_t nsteps);
 /* garment = -1: all garments concatenated in id order. */
 int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device);
 int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]);
+/* visg_set_vertices over the whole batch: idx are global vertex indices (garments
+ * concatenated in id order). */
+int visg_batch_set_vertices(VisgBatch* b, const uint32_t* idx, const float* xyz, int32_t n);
 int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* body_xyz,
                            const float* body_normals);
 /* Times the candidate launch shapes of the step kernel on this batch's own data
@@ -209,6 +220,7 @@ int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* body_xyz,
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm);
 int visg_batch_info(VisgBatch* b, int32_t* n_garments, int64_t* n_vertices,
                     int64_t* n_entries, int64_t* n_tris);
+int visg_batch_count_contacts(VisgBatch* b, int64_t* n);
 int visg_batch_sync(VisgBatch* b);
 int visg_batch_destroy(VisgBatch* b);
 

@@ -61,10 +61,14 @@ def lib():
         "visg_update_body_device": (C.c_int, [_vp, _vp, _vp]),
         "visg_set_vertex": (C.c_int, [_vp, C.c_uint32, _fp]),
         "visg_set_pinned": (C.c_int, [_vp, _u32p, C.c_int32]),
+        "visg_set_vertices": (C.c_int, [_vp, _u32p, _fp, C.c_int32]),
+        "visg_batch_set_vertices": (C.c_int, [_vp, _u32p, _fp, C.c_int32]),
         "visg_get_positions": (C.c_int, [_vp, _vp, C.c_int32]),
         "visg_get_state": (C.c_int, [_vp, _fp, _fp, _fp]),
         "visg_set_state": (C.c_int, [_vp, _fp, _fp, _fp]),
         "visg_sync": (C.c_int, [_vp]),
+        "visg_count_contacts": (C.c_int, [_vp, _i64p]),
+        "visg_batch_count_contacts": (C.c_int, [_vp, _i64p]),
         "visg_get_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p]),
         "visg_export_lbvh": (C.c_int, [_vp, _u32p, _fp, _u32p, _i32p, _i32p, _i32p, _i32p, _i32p, _fp, _fp, _fp]),
         "visg_query_points": (C.c_int, [_vp, _fp, C.c_int32, _i32p, _i32p, _fp, _fp]),
@@ -175,6 +179,11 @@ class Simulator:
         v = _f32(new_value).reshape(3)
         _check(lib().visg_set_vertex(self.h, idx, _p(v)))
 
+    def update_vertices(self, idx, xyz):
+        a = np.ascontiguousarray(idx, np.uint32)
+        v = _f32(xyz).reshape(-1, 3)
+        _check(lib().visg_set_vertices(self.h, _p(a, _u32p), _p(v), len(a)))
+
     def update_body(self, xyz, normals=None):
         _check(lib().visg_update_body(self.h, _p(_f32(xyz)), _p(_f32(normals))))
 
@@ -206,6 +215,11 @@ class Simulator:
 
     def sync(self):
         _check(lib().visg_sync(self.h))
+
+    def count_contacts(self) -> int:
+        n = C.c_int64()
+        _check(lib().visg_count_contacts(self.h, C.byref(n)))
+        return n.value
 
     def info(self):
         a, b, c, d = (C.c_int32() for _ in range(4))
@@ -299,6 +313,12 @@ class BatchSimulator:
         v = _f32(new_value).reshape(3)
         _check(lib().visg_batch_set_vertex(self.h, garment, idx, _p(v)))
 
+    def update_vertices(self, idx, xyz):
+        """idx: global vertex indices (garments concatenated in id order)."""
+        a = np.ascontiguousarray(idx, np.uint32)
+        v = _f32(xyz).reshape(-1, 3)
+        _check(lib().visg_batch_set_vertices(self.h, _p(a, _u32p), _p(v), len(a)))
+
     def update_body(self, garment: int, xyz, normals=None):
         _check(lib().visg_batch_update_body(self.h, garment, _p(_f32(xyz)), _p(_f32(normals))))
 
@@ -315,6 +335,11 @@ class BatchSimulator:
 
     def sync(self):
         _check(lib().visg_batch_sync(self.h))
+
+    def count_contacts(self) -> int:
+        n = C.c_int64()
+        _check(lib().visg_batch_count_contacts(self.h, C.byref(n)))
+        return n.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -144,7 +144,11 @@ struct Engine {
 
     ~Engine() {
         if (stream) cudaStreamSynchronize(stream);
+        cudaDeviceSynchronize();
         destroy_graphs();
+        if (d_sv_idx) cudaFree(d_sv_idx);
+        if (h_sv) cudaFreeHost(h_sv);
+        if (sv_done) cudaEventDestroy(sv_done);
         free_adjoint();
         arena.release();
         if (h_status) cudaFreeHost(h_status);
@@ -509,6 +513,41 @@ struct Engine {
         return VISG_OK;
     }
 
+    // many vertices at once: host arrays staged into a pinned buffer, one H2D, one scatter
+    uint32_t* d_sv_idx = nullptr;
+    float* d_sv_xyz = nullptr;
+    char* h_sv = nullptr;
+    int sv_cap = 0;
+    cudaEvent_t sv_done = nullptr;
+    int set_vertices(const uint32_t* idx, const float* xyz, int n) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (n < 0 || (n > 0 && (!idx || !xyz))) return fail(VISG_ERR_INVALID_ARG, "bad vertex list");
+        for (int k = 0; k < n; ++k)
+            if (idx[k] >= (uint64_t)N) return fail(VISG_ERR_INVALID_ARG, "vertex index out of range");
+        if (n == 0) return VISG_OK;
+        if (n > sv_cap) {
+            if (sv_done) CU(cudaEventSynchronize(sv_done));
+            cudaFree(d_sv_idx);
+            cudaFreeHost(h_sv);
+            d_sv_idx = nullptr;
+            h_sv = nullptr;
+            int cap = std::max(n, 1024);
+            CU(cudaMalloc((void**)&d_sv_idx, (size_t)cap * 16));
+            d_sv_xyz = (float*)(d_sv_idx + cap);
+            CU(cudaHostAlloc((void**)&h_sv, (size_t)cap * 16, cudaHostAllocDefault));
+            if (!sv_done) CU(cudaEventCreateWithFlags(&sv_done, cudaEventDisableTiming));
+            sv_cap = cap;
+        }
+        CU(cudaEventSynchronize(sv_done));  // the previous upload has left the staging buffer
+        std::memcpy(h_sv, idx, (size_t)n * 4);
+        std::memcpy(h_sv + (size_t)sv_cap * 4, xyz, (size_t)n * 12);
+        CU(cudaMemcpyAsync(d_sv_idx, h_sv, (size_t)n * 4, cudaMemcpyHostToDevice, stream));
+        CU(cudaMemcpyAsync(d_sv_xyz, h_sv + (size_t)sv_cap * 4, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
+        CU(cudaEventRecord(sv_done, stream));
+        CU(launch_set_vertices(d_state[cur], d_sv_idx, d_sv_xyz, n, stream));
+        return VISG_OK;
+    }
+
     int set_pinned(const uint32_t* idx, int n) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         if (n < 0 || (n > 0 && !idx)) return fail(VISG_ERR_INVALID_ARG, "bad pin list");
@@ -536,6 +575,19 @@ struct Engine {
         }
         CU(launch_unpack_positions(d_state[cur] + 2 * v0, n, d_stage, stream));
         CU(cudaMemcpyAsync(out, d_stage, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
+        return sync();
+    }
+
+    int count_contacts(int64_t* out) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
+        unsigned long long* d = (unsigned long long*)d_stage;
+        CU(cudaMemsetAsync(d, 0, 8, stream));
+        CU(launch_count_contacts(d_state[cur], N, d, stream));
+        unsigned long long h = 0;
+        CU(cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, stream));
+        CU(cudaStreamSynchronize(stream));
+        *out = (int64_t)h;
         return sync();
     }
 
@@ -861,6 +913,11 @@ int visg_set_vertex(VisgSim* sim, uint32_t idx, const float xyz[3]) {
     return sim->eng.set_vertex(0, idx, xyz);
 }
 
+int visg_set_vertices(VisgSim* sim, const uint32_t* idx, const float* xyz, int32_t n) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.set_vertices(idx, xyz, n);
+}
+
 int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.set_pinned(idx, n);
@@ -884,6 +941,16 @@ int visg_set_state(VisgSim* sim, const float* x, const float* xo, const float* n
 int visg_sync(VisgSim* sim) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.sync();
+}
+
+int visg_count_contacts(VisgSim* sim, int64_t* n) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.count_contacts(n);
+}
+
+int visg_batch_count_contacts(VisgBatch* b, int64_t* n) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.count_contacts(n);
 }
 
 int visg_get_info(VisgSim* sim, int32_t* nv, int32_t* ne, int32_t* nt, int32_t* nl) {
@@ -975,6 +1042,11 @@ int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t 
 int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.set_vertex(garment, idx, xyz);
+}
+
+int visg_batch_set_vertices(VisgBatch* b, const uint32_t* idx, const float* xyz, int32_t n) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.set_vertices(idx, xyz, n);
 }
 
 int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* xyz, const float* nrm) {

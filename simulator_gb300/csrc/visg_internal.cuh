@@ -147,6 +147,12 @@ cudaError_t launch_unpack_state(const float4* state, const float4* normal, int64
 cudaError_t launch_pack_state(float4* state, float4* normal, int64_t n, const float* x, const float* xo,
                               const float* nrm, cudaStream_t s);
 
+// number of vertices with the contact flag set, accumulated into *count
+cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long long* count, cudaStream_t s);
+
+// scatter (idx[k] -> x = x_old = xyz[k]) into the state, keeping the contact flag
+cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, cudaStream_t s);
+
 // ---- adjoint ---------------------------------------------------------------------------
 struct AdjArgs {
     const float4* state;    // the step's input state (x, x_old, flags)

@@ -282,6 +282,25 @@ __global__ void k_pack_state(float4* st, float4* nr, int64_t n, const float* x, 
     st[2 * i + 1] = s1;
 }
 
+__global__ void k_set_vertices(float4* st, const uint32_t* __restrict__ idx, const float* __restrict__ xyz, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int64_t v = idx[k];
+    const float x = xyz[3 * k], y = xyz[3 * k + 1], z = xyz[3 * k + 2];
+    st[2 * v] = make_float4(x, y, z, x);
+    float4 s1 = st[2 * v + 1];
+    s1.x = y;
+    s1.y = z;
+    st[2 * v + 1] = s1;
+}
+
+__global__ void k_count_contacts(const float4* __restrict__ st, int64_t n, unsigned long long* count) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool c = i < n && (__float_as_uint(st[2 * i + 1].z) & FLAG_HAS_NORMAL);
+    const unsigned m = __ballot_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+}
+
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
 }  // namespace
@@ -323,6 +342,18 @@ cudaError_t launch_unpack_state(const float4* state, const float4* normal, int64
                                 cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     k_unpack_state<<<grid_for(n, 256), 256, 0, s>>>(state, normal, n, x, xo, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long long* count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_count_contacts<<<grid_for(n, 256), 256, 0, s>>>(state, n, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_set_vertices<<<grid_for(n, 256), 256, 0, s>>>(state, idx, xyz, n);
     return cudaGetLastError();
 }
 

@@ -263,10 +263,11 @@ def sheet_over_sphere(side: int = 64, subdiv: int = 4, radius: float = 0.3, seed
 
 
 def garment_batch(n_garments: int = 256, seed: int = 0, side_range=(32, 256), subdiv_range=(3, 6),
-                  radius_range=(0.2, 0.4)):
-    """Per garment: side ~ U{32..256}, a 1 m sheet with the three spring families,
-    facing an icosphere of subdivision ~ U{3..6} and radius ~ U[0.2, 0.4] placed
-    radius + 0.2 m below the sheet."""
+                  radius_range=(0.2, 0.4), cap: float = 0.05):
+    """Per garment: side ~ U{32..256}, a 1 m sheet with the three spring families and
+    two pinned corners, facing an icosphere of subdivision ~ U{3..6} and radius
+    ~ U[0.2, 0.4] m whose top rises `cap` metres through the sheet (the sheet starts
+    draped over the sphere's cap, so the collision path is exercised from step 1)."""
     rng = np.random.default_rng(seed)
     sides = rng.integers(side_range[0], side_range[1] + 1, size=n_garments)
     subs = rng.integers(subdiv_range[0], subdiv_range[1] + 1, size=n_garments)
@@ -280,7 +281,7 @@ def garment_batch(n_garments: int = 256, seed: int = 0, side_range=(32, 256), su
             spheres[key] = icosphere(key, 1.0)
         unit = spheres[key]
         r = float(radii[g])
-        body = Body(xyz=(unit.xyz.astype(np.float64) * r + np.array([0.0, -(r + 0.2), 0.0])).astype(np.float32),
+        body = Body(xyz=(unit.xyz.astype(np.float64) * r + np.array([0.0, cap - r, 0.0])).astype(np.float32),
                     tris=unit.tris, normals=unit.normals)
         out.append((cloth, body))
     return out

@@ -37,7 +37,7 @@ def soup(n_tris: int, seed: int, spread: float = 1.0, dup_frac: float = 0.0):
     return xyz, tris
 
 
-def ref_scene(side=24, subdiv=2, radius=0.3, drop=0.35, lists="grid"):
+def ref_scene(side=24, subdiv=2, radius=0.3, drop=0.31, lists="grid"):
     """Sheet above an icosphere with the reference's constants; lists = 'grid'
     (3 families) or 'mesh' (the reference's structure + bend lists)."""
     cloth = scenes.grid_cloth(side, 1.0, 0.0, pin_top_corners=False)
