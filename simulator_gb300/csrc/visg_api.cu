@@ -305,12 +305,15 @@ struct Engine {
         CU(arena.commit());
         // upload
         std::vector<float4> st(2 * (size_t)N);
+        float xo_is_x_bits;
+        const uint32_t fl0 = FLAG_XO_IS_X;
+        std::memcpy(&xo_is_x_bits, &fl0, 4);
         for (int g = 0; g < G; ++g)
             for (int i = 0; i < gin[g].N; ++i) {
                 const float* q = &gin[g].xyz[3 * (size_t)i];
                 int64_t v = voff[g] + i;
-                st[2 * v] = make_float4(q[0], q[1], q[2], q[0]);
-                st[2 * v + 1] = make_float4(q[1], q[2], 0.0f, 0.0f);
+                st[2 * v] = make_float4(q[0], q[1], q[2], 0.0f);  // x = x_old: v = 0 (simulation.cu:84-85)
+                st[2 * v + 1] = make_float4(0.0f, 0.0f, xo_is_x_bits, 0.0f);
             }
         CU(cudaMemcpy(d_state[0], st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(d_rowp, h_rowp.data(), h_rowp.size() * 4, cudaMemcpyHostToDevice));
@@ -348,6 +351,9 @@ struct Engine {
         if (p.verlet_damping == 1.0f) v |= SV_REFV;
         if (p.collide && any_body) v |= SV_COLLIDE;
         if (p.check_every > 0) v |= SV_CHECK;
+        uint32_t kdbits;
+        std::memcpy(&kdbits, &p.spring_damping, 4);
+        if (kdbits == 0u) v |= SV_KD0;
         return v;
     }
 
@@ -507,8 +513,8 @@ struct Engine {
         int64_t v;
         if (int r = check_vertex(g, idx, &v)) return r;
         if (!xyz) return fail(VISG_ERR_INVALID_ARG, "xyz is NULL");
-        float rec[6] = {xyz[0], xyz[1], xyz[2], xyz[0], xyz[1], xyz[2]};  // x and x_old (simulation.cu:255-256)
-        CU(cudaMemcpyAsync(&d_state[cur][2 * v], rec, sizeof rec, cudaMemcpyHostToDevice, stream));
+        const uint32_t gi = (uint32_t)v;  // x and x_old (simulation.cu:255-256)
+        if (int r = set_vertices(&gi, xyz, 1)) return r;
         CU(cudaStreamSynchronize(stream));
         return VISG_OK;
     }
@@ -544,7 +550,7 @@ struct Engine {
         CU(cudaMemcpyAsync(d_sv_idx, h_sv, (size_t)n * 4, cudaMemcpyHostToDevice, stream));
         CU(cudaMemcpyAsync(d_sv_xyz, h_sv + (size_t)sv_cap * 4, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
         CU(cudaEventRecord(sv_done, stream));
-        CU(launch_set_vertices(d_state[cur], d_sv_idx, d_sv_xyz, n, stream));
+        CU(launch_set_vertices(d_state[cur], d_sv_idx, d_sv_xyz, n, p.dt, stream));
         return VISG_OK;
     }
 
@@ -596,7 +602,7 @@ struct Engine {
         float* sx = d_stage;
         float* sxo = d_stage + 3 * N;
         float* sn = d_stage + 6 * N;
-        CU(launch_unpack_state(d_state[cur], d_normal, N, sx, sxo, sn, stream));
+        CU(launch_unpack_state(d_state[cur], d_state[cur ^ 1], d_normal, N, sx, sxo, sn, stream));
         if (x) CU(cudaMemcpyAsync(x, sx, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
         if (xo) CU(cudaMemcpyAsync(xo, sxo, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
         if (nrm) CU(cudaMemcpyAsync(nrm, sn, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
@@ -611,7 +617,8 @@ struct Engine {
         if (x) CU(cudaMemcpyAsync(sx, x, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
         if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
         if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
-        CU(launch_pack_state(d_state[cur], d_normal, N, x ? sx : nullptr, xo ? sxo : nullptr, nrm ? sn : nullptr,
+        CU(launch_pack_state(d_state[cur], d_state[cur ^ 1], d_normal, N, x ? sx : nullptr, xo ? sxo : nullptr,
+                             nrm ? sn : nullptr, p.dt,
                              stream));
         CU(cudaStreamSynchronize(stream));
         return VISG_OK;
@@ -744,7 +751,7 @@ struct Engine {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         if (int r = sync()) return r;
         float4 *bs = nullptr, *bn = nullptr;
-        CU(cudaMalloc((void**)&bs, 2 * (size_t)N * sizeof(float4)));
+        CU(cudaMalloc((void**)&bs, 4 * (size_t)N * sizeof(float4)));
         cudaError_t e = cudaMalloc((void**)&bn, (size_t)N * sizeof(float4));
         if (e != cudaSuccess) {
             cudaFree(bs);
@@ -752,6 +759,9 @@ struct Engine {
         }
         const int cur0 = cur;
         e = cudaMemcpyAsync(bs, d_state[cur], 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(bs + 2 * N, d_state[cur ^ 1], 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(bn, d_normal, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
@@ -791,6 +801,9 @@ struct Engine {
         cur = cur0;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(d_state[cur], bs, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_state[cur ^ 1], bs + 2 * N, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d_normal, bn, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         cudaEventDestroy(e0);

@@ -2,7 +2,9 @@
 //
 // HBM layout (all arrays 16-byte aligned, one allocation per engine):
 //   cloth state, double-buffered: 2 float4 per vertex
-//        [x.x x.y x.z xo.x] [xo.y xo.z flags 0]          32 B, one sector per gather
+//        [x.x x.y x.z v.x] [v.y v.z flags 0]             32 B, one sector per gather
+//        v = (x - x_old) / dt, computed once per step by the vertex's own thread;
+//        x_old is x (flag XO_IS_X) or the x of the same vertex in the other buffer
 //   contact normal (previous step):  float4 per vertex, read only when flags says so
 //   rowp:   u32 per vertex + 1, merged CSR row offsets; bit 31 = vertex pinned
 //   ent:    uint2 per directed spring {end | list << 30, rest}         8 B
@@ -28,7 +30,8 @@ constexpr uint32_t PIN_BIT = 0x80000000u;
 constexpr uint32_t ROW_MASK = 0x7fffffffu;
 constexpr uint32_t END_MASK = 0x3fffffffu;
 constexpr int LIST_SHIFT = 30;
-constexpr uint32_t FLAG_HAS_NORMAL = 1u;
+constexpr uint32_t FLAG_HAS_NORMAL = 1u;  // the previous contact normal is stored (non-zero)
+constexpr uint32_t FLAG_XO_IS_X = 2u;     // x_old equals x (else x_old = x of the other buffer)
 
 // error bits written by kernels into the engine's error word
 constexpr int ERR_STACK = 1;     // traversal stack would overflow (not reachable for <= 30-bit codes)
@@ -132,6 +135,7 @@ enum StepVariant : int {
     SV_REFV = 2,      // reference Verlet expression (gamma == 1)
     SV_COLLIDE = 4,   // body collision
     SV_CHECK = 8,     // divergence check
+    SV_KD0 = 16,      // spring damping exactly +0
 };
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
 int step_max_ctas_per_sm(int variant, int block);
@@ -142,16 +146,18 @@ cudaError_t launch_query(BvhView v, const float* pts, int n, int* leaf, int* ins
 
 // unpack positions of vertices [0, n) into packed xyz
 cudaError_t launch_unpack_positions(const float4* state, int64_t n, float* out, cudaStream_t s);
-cudaError_t launch_unpack_state(const float4* state, const float4* normal, int64_t n, float* x, float* xo,
-                                float* nrm, cudaStream_t s);
-cudaError_t launch_pack_state(float4* state, float4* normal, int64_t n, const float* x, const float* xo,
-                              const float* nrm, cudaStream_t s);
+cudaError_t launch_unpack_state(const float4* state, const float4* other, const float4* normal, int64_t n, float* x,
+                                float* xo, float* nrm, cudaStream_t s);
+// x/xo/nrm may be NULL (kept); dt recomputes v = (x - x_old) / dt
+cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x,
+                              const float* xo, const float* nrm, float dt, cudaStream_t s);
 
 // number of vertices with the contact flag set, accumulated into *count
 cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long long* count, cudaStream_t s);
 
 // scatter (idx[k] -> x = x_old = xyz[k]) into the state, keeping the contact flag
-cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, cudaStream_t s);
+cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt,
+                                cudaStream_t s);
 
 // ---- adjoint ---------------------------------------------------------------------------
 struct AdjArgs {

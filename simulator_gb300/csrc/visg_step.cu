@@ -76,11 +76,102 @@ __device__ __forceinline__ int query_leaf(const BvhView& bv, int n_leaves, int r
     return first_hit(bv.nodes, root, n_leaves, p, err);
 }
 
-template <int BLOCK, bool PERK, bool COLL>
-__global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check) {
+// Force of one CSR spring on the vertex at x moving with velocity vel (verlet.cu:64-84).
+// t0/t1 is the neighbour's record: position and velocity (p2 - p2_old) / dt, stored
+// once per step by the neighbour's own thread with the same IEEE division.
+// With KD0 (spring damping exactly +0) the damping term is +0 * RN(dot / dist), a
+// signed zero: left + (+-0) == left for every finite non-zero left, so the damping
+// term is evaluated only when left is zero or not finite.
+template <bool KD0>
+__device__ __forceinline__ f3 spring_force(f3 x, f3 vel, float4 t0, float4 t1, float ks, float rest, float kd,
+                                           f3 eps3) {
+    const f3 p2 = mk3(t0.x, t0.y, t0.z);
+    const f3 dP = add(sub(x, p2), eps3);
+    const float dist = __fsqrt_rn(dot(dP, dP));
+    const float left = __fmul_rn(-ks, __fsub_rn(dist, rest));
+    float c;
+    if (KD0 && left != 0.0f && isfinite(left)) {
+        c = left;
+    } else {
+        const f3 dV = sub(vel, mk3(t0.w, t1.x, t1.y));
+        c = __fadd_rn(left, __fmul_rn(kd, __fdiv_rn(dot(dV, dP), dist)));
+    }
+    return mul(c, mul(dP, __frcp_rn(dist)));  // normalize(dP) = dP * (1 / |dP|)
+}
+
+__device__ __forceinline__ float pick(int f, float k0, float k1, float k2, float k3) {
+    return f == 0 ? k0 : (f == 1 ? k1 : (f == 2 ? k2 : k3));
+}
+
+struct SpringIn {
+    uint2 en;
+    float4 t0, t1;
+    float k;
+};
+
+__device__ __forceinline__ SpringIn load_spring(const StepArgs& a, const float4* __restrict__ sin, uint32_t e,
+                                                bool perk) {
+    SpringIn s;
+    s.en = __ldg(&a.ent[e]);
+    const int j = (int)(s.en.x & END_MASK);
+    s.t0 = __ldg(&sin[2 * j]);
+    s.t1 = __ldg(&sin[2 * j + 1]);
+    s.k = perk ? __ldg(&a.kent[e]) : 0.0f;
+    return s;
+}
+
+// Sum of the spring forces of row [rp, re) into F, list by list as the reference
+// does (force += list sum, verlet.cu:148-149), entries in CSR order.  Springs are
+// evaluated two at a time (independent chains) and accumulated in order.
+template <bool KD0>
+__device__ __forceinline__ f3 spring_sum(const StepArgs& a, const float4* __restrict__ sin, uint32_t rp,
+                                         uint32_t re, f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
+    const float k0 = P.list_k[0], k1 = P.list_k[1], k2 = P.list_k[2], k3 = P.list_k[3];
+    f3 acc = mk3(0.0f, 0.0f, 0.0f);
+    int list = 0;
+    auto take = [&](const SpringIn& s, f3 sf) {
+        const int f = (int)(s.en.x >> LIST_SHIFT);
+        while (list < f) {
+            F = add(F, acc);
+            acc = mk3(0.0f, 0.0f, 0.0f);
+            ++list;
+        }
+        acc = add(acc, sf);
+    };
+    uint32_t e = rp;
+    for (; e + 1 < re; e += 2) {
+        const SpringIn sa = load_spring(a, sin, e, perk);
+        const SpringIn sb = load_spring(a, sin, e + 1, perk);
+        const float ka = perk ? sa.k : pick((int)(sa.en.x >> LIST_SHIFT), k0, k1, k2, k3);
+        const float kb = perk ? sb.k : pick((int)(sb.en.x >> LIST_SHIFT), k0, k1, k2, k3);
+        const f3 fa = spring_force<KD0>(x, vel, sa.t0, sa.t1, ka, __uint_as_float(sa.en.y), P.kd, eps3);
+        const f3 fb = spring_force<KD0>(x, vel, sb.t0, sb.t1, kb, __uint_as_float(sb.en.y), P.kd, eps3);
+        take(sa, fa);
+        take(sb, fb);
+    }
+    if (e < re) {
+        const SpringIn sa = load_spring(a, sin, e, perk);
+        const float ka = perk ? sa.k : pick((int)(sa.en.x >> LIST_SHIFT), k0, k1, k2, k3);
+        take(sa, spring_force<KD0>(x, vel, sa.t0, sa.t1, ka, __uint_as_float(sa.en.y), P.kd, eps3));
+    }
+    while (list < P.n_lists) {
+        F = add(F, acc);
+        acc = mk3(0.0f, 0.0f, 0.0f);
+        ++list;
+    }
+    return F;
+}
+
+// State record of vertex i in buffer b: [x.xyz, v.x] [v.y, v.z, flags, 0] with
+// v = (x - x_old) / dt.  x_old is x itself when FLAG_XO_IS_X is set (after a
+// contact, a pin or update_vertex) and otherwise the previous step's x, which is
+// still in the other buffer: the step reads it there before overwriting it.
+template <int BLOCK, bool COLL, bool KD0>
+__global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
     const StepParams& P = a.p;
     const f3 grav = mk3(P.gx, P.gy, P.gz);
     const f3 eps3 = mk3(kFltEpsilon, kFltEpsilon, kFltEpsilon);
+    const float4* __restrict__ sin = a.state_in;
     float my_disp = 0.0f;
     uint32_t my_bad = 0;
     for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
@@ -88,10 +179,10 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
         const int i = td.y + (int)threadIdx.x;
         const bool active = i < td.z;
         const int ii = active ? i : td.y;
-        const float4 s0 = __ldg(&a.state_in[2 * ii]);
-        const float4 s1 = __ldg(&a.state_in[2 * ii + 1]);
+        const float4 s0 = __ldg(&sin[2 * ii]);
+        const float4 s1 = __ldg(&sin[2 * ii + 1]);
         const f3 x = mk3(s0.x, s0.y, s0.z);
-        const f3 xo = mk3(s0.w, s1.x, s1.y);
+        const f3 vel = mk3(s0.w, s1.x, s1.y);
         const uint32_t flags = __float_as_uint(s1.z);
         uint32_t rp = __ldg(&a.rowp[ii]);
         const uint32_t re = __ldg(&a.rowp[ii + 1]) & ROW_MASK;
@@ -100,39 +191,11 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
         f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
         bool has_n = false;
         if (!pinned) {
+            const f3 xo = (flags & FLAG_XO_IS_X) ? x : xyz(a.state_out[2 * ii]);
             f3 np = mk3(0.0f, 0.0f, 0.0f);
             if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
-            const f3 vel = divs(sub(x, xo), P.dt);
             f3 F = add(mul(grav, P.mass), mul(vel, P.damp));
-            f3 acc = mk3(0.0f, 0.0f, 0.0f);
-            int list = 0;
-            for (uint32_t e = rp; e < re; ++e) {
-                const uint2 en = __ldg(&a.ent[e]);
-                const int j = (int)(en.x & END_MASK);
-                const int f = (int)(en.x >> LIST_SHIFT);
-                while (list < f) {  // list boundary: force += that list's sum (verlet.cu:148-149)
-                    F = add(F, acc);
-                    acc = mk3(0.0f, 0.0f, 0.0f);
-                    ++list;
-                }
-                const float ks = PERK ? __ldg(&a.kent[e]) : P.list_k[f];
-                const float4 t0 = __ldg(&a.state_in[2 * j]);
-                const float4 t1 = __ldg(&a.state_in[2 * j + 1]);
-                const f3 p2 = mk3(t0.x, t0.y, t0.z);
-                const f3 p2o = mk3(t0.w, t1.x, t1.y);
-                const f3 v2 = divs(sub(p2, p2o), P.dt);
-                const f3 dP = add(sub(x, p2), eps3);
-                const f3 dV = sub(vel, v2);
-                const float dist = length(dP);
-                const float left = __fmul_rn(-ks, __fsub_rn(dist, __uint_as_float(en.y)));
-                const float right = __fmul_rn(P.kd, __fdiv_rn(dot(dV, dP), dist));
-                acc = add(acc, mul(__fadd_rn(left, right), normalize(dP)));
-            }
-            while (list < P.n_lists) {
-                F = add(F, acc);
-                acc = mk3(0.0f, 0.0f, 0.0f);
-                ++list;
-            }
+            F = spring_sum<KD0>(a, sin, rp, re, x, vel, F, P, perk != 0, eps3);
             F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
             const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
             if (refv) xn = add(sub(add(x, x), xo), adt);
@@ -166,13 +229,17 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
             }
         }
         if (active) {
-            a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, xon.x);
-            a.state_out[2 * i + 1] = make_float4(xon.y, xon.z, __uint_as_float(has_n ? FLAG_HAS_NORMAL : 0u), 0.0f);
+            const bool xo_is_x = pinned || has_n;
+            const f3 vn = divs(sub(xn, xon), P.dt);
+            const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u);
+            a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, vn.x);
+            a.state_out[2 * i + 1] = make_float4(vn.y, vn.z, __uint_as_float(fl), 0.0f);
             if (has_n) a.normal[i] = make_float4(nn.x, nn.y, nn.z, 0.0f);
             if (check) {
-                const float dd = fmaxf(fabsf(__fsub_rn(xn.x, x.x)), fmaxf(fabsf(__fsub_rn(xn.y, x.y)), fabsf(__fsub_rn(xn.z, x.z))));
-                if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(xon.x) || !isfinite(xon.y) ||
-                    !isfinite(xon.z))
+                const float dd = fmaxf(fabsf(__fsub_rn(xn.x, x.x)),
+                                       fmaxf(fabsf(__fsub_rn(xn.y, x.y)), fabsf(__fsub_rn(xn.z, x.z))));
+                if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(vn.x) || !isfinite(vn.y) ||
+                    !isfinite(vn.z))
                     ++my_bad;
                 else
                     my_disp = fmaxf(my_disp, dd);
@@ -192,27 +259,35 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
     }
 }
 
-template <int BLOCK>
-cudaError_t launch_block(const StepArgs& a, int variant, int grid, cudaStream_t s) {
-    const int refv = (variant & SV_REFV) ? 1 : 0;
-    const int check = (variant & SV_CHECK) ? 1 : 0;
-    const bool perk = (variant & SV_PERK) != 0, coll = (variant & SV_COLLIDE) != 0;
-    if (perk && coll) k_step<BLOCK, true, true><<<grid, BLOCK, 0, s>>>(a, refv, check);
-    else if (perk) k_step<BLOCK, true, false><<<grid, BLOCK, 0, s>>>(a, refv, check);
-    else if (coll) k_step<BLOCK, false, true><<<grid, BLOCK, 0, s>>>(a, refv, check);
-    else k_step<BLOCK, false, false><<<grid, BLOCK, 0, s>>>(a, refv, check);
+template <int BLOCK, bool KD0>
+cudaError_t launch_kd(const StepArgs& a, bool coll, int refv, int check, int perk, int grid, cudaStream_t s) {
+    if (coll) k_step<BLOCK, true, KD0><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
+    else k_step<BLOCK, false, KD0><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
     return cudaGetLastError();
 }
 
 template <int BLOCK>
-int occupancy_block(int variant) {
+cudaError_t launch_block(const StepArgs& a, int variant, int grid, cudaStream_t s) {
+    const int refv = (variant & SV_REFV) ? 1 : 0;
+    const int check = (variant & SV_CHECK) ? 1 : 0;
+    const int perk = (variant & SV_PERK) ? 1 : 0;
+    const bool coll = (variant & SV_COLLIDE) != 0;
+    if (variant & SV_KD0) return launch_kd<BLOCK, true>(a, coll, refv, check, perk, grid, s);
+    return launch_kd<BLOCK, false>(a, coll, refv, check, perk, grid, s);
+}
+
+template <int BLOCK, bool KD0>
+int occupancy_kd(bool coll) {
     int n = 0;
-    const bool perk = (variant & SV_PERK) != 0, coll = (variant & SV_COLLIDE) != 0;
-    if (perk && coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, true>, BLOCK, 0);
-    else if (perk) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, false>, BLOCK, 0);
-    else if (coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, true>, BLOCK, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, false>, BLOCK, 0);
+    if (coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, KD0>, BLOCK, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, KD0>, BLOCK, 0);
     return n;
+}
+
+template <int BLOCK>
+int occupancy_block(int variant) {
+    const bool coll = (variant & SV_COLLIDE) != 0;
+    return (variant & SV_KD0) ? occupancy_kd<BLOCK, true>(coll) : occupancy_kd<BLOCK, false>(coll);
 }
 
 __global__ void k_query(BvhView bv, const float* __restrict__ pts, int n, int* leaf, int* inside, float* dist,
@@ -250,48 +325,46 @@ __global__ void k_unpack_positions(const float4* __restrict__ st, int64_t n, flo
     out[3 * i + 2] = s0.z;
 }
 
-__global__ void k_unpack_state(const float4* __restrict__ st, const float4* __restrict__ nr, int64_t n, float* x,
-                               float* xo, float* nrm) {
+__global__ void k_unpack_state(const float4* __restrict__ st, const float4* __restrict__ other,
+                               const float4* __restrict__ nr, int64_t n, float* x, float* xo, float* nrm) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 s0 = st[2 * i], s1 = st[2 * i + 1];
+    const uint32_t fl = __float_as_uint(s1.z);
     if (x) { x[3 * i] = s0.x; x[3 * i + 1] = s0.y; x[3 * i + 2] = s0.z; }
-    if (xo) { xo[3 * i] = s0.w; xo[3 * i + 1] = s1.x; xo[3 * i + 2] = s1.y; }
+    if (xo) {
+        const float4 o = (fl & FLAG_XO_IS_X) ? s0 : other[2 * i];
+        xo[3 * i] = o.x; xo[3 * i + 1] = o.y; xo[3 * i + 2] = o.z;
+    }
     if (nrm) {
-        const bool h = (__float_as_uint(s1.z) & FLAG_HAS_NORMAL) != 0u;
-        const float4 v = h ? nr[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 v = (fl & FLAG_HAS_NORMAL) ? nr[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         nrm[3 * i] = v.x; nrm[3 * i + 1] = v.y; nrm[3 * i + 2] = v.z;
     }
 }
 
-// x == nullptr keeps x, etc.  A vertex has a stored normal iff it is non-zero.
-__global__ void k_pack_state(float4* st, float4* nr, int64_t n, const float* x, const float* xo, const float* nrm) {
+// x == nullptr keeps x, etc.  x_old is written into the other buffer and v is
+// recomputed as (x - x_old) / dt; a vertex has a stored normal iff it is non-zero.
+__global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, const float* x, const float* xo,
+                             const float* nrm, float dt) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 s0 = st[2 * i], s1 = st[2 * i + 1];
-    if (x) { s0.x = x[3 * i]; s0.y = x[3 * i + 1]; s0.z = x[3 * i + 2]; }
-    if (xo) { s0.w = xo[3 * i]; s1.x = xo[3 * i + 1]; s1.y = xo[3 * i + 2]; }
+    uint32_t fl = __float_as_uint(s1.z);
+    const f3 x0 = mk3(s0.x, s0.y, s0.z);
+    const f3 xo0 = (fl & FLAG_XO_IS_X) ? x0 : xyz(other[2 * i]);
+    const f3 xv = x ? mk3(x[3 * i], x[3 * i + 1], x[3 * i + 2]) : x0;
+    const f3 xov = xo ? mk3(xo[3 * i], xo[3 * i + 1], xo[3 * i + 2]) : xo0;
+    const f3 v = divs(sub(xv, xov), dt);
     if (nrm) {
         const float a = nrm[3 * i], b = nrm[3 * i + 1], c = nrm[3 * i + 2];
         const bool h = a != 0.0f || b != 0.0f || c != 0.0f;
         nr[i] = make_float4(a, b, c, 0.0f);
-        s1.z = __uint_as_float(h ? FLAG_HAS_NORMAL : 0u);
+        fl = (fl & ~FLAG_HAS_NORMAL) | (h ? FLAG_HAS_NORMAL : 0u);
     }
-    s1.w = 0.0f;
-    st[2 * i] = s0;
-    st[2 * i + 1] = s1;
-}
-
-__global__ void k_set_vertices(float4* st, const uint32_t* __restrict__ idx, const float* __restrict__ xyz, int n) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int64_t v = idx[k];
-    const float x = xyz[3 * k], y = xyz[3 * k + 1], z = xyz[3 * k + 2];
-    st[2 * v] = make_float4(x, y, z, x);
-    float4 s1 = st[2 * v + 1];
-    s1.x = y;
-    s1.y = z;
-    st[2 * v + 1] = s1;
+    fl &= ~FLAG_XO_IS_X;
+    other[2 * i] = make_float4(xov.x, xov.y, xov.z, 0.0f);
+    st[2 * i] = make_float4(xv.x, xv.y, xv.z, v.x);
+    st[2 * i + 1] = make_float4(v.y, v.z, __uint_as_float(fl), 0.0f);
 }
 
 __global__ void k_count_contacts(const float4* __restrict__ st, int64_t n, unsigned long long* count) {
@@ -299,6 +372,20 @@ __global__ void k_count_contacts(const float4* __restrict__ st, int64_t n, unsig
     const bool c = i < n && (__float_as_uint(st[2 * i + 1].z) & FLAG_HAS_NORMAL);
     const unsigned m = __ballot_sync(0xffffffffu, c);
     if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+}
+
+// update_vertex (simulation.cu:253-257): x = x_old = p, so v = (p - p) / dt; the
+// stored contact normal is kept
+__global__ void k_set_vertices(float4* st, const uint32_t* __restrict__ idx, const float* __restrict__ xyz3, int n,
+                               float dt) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int64_t v = idx[k];
+    const f3 p = mk3(xyz3[3 * k], xyz3[3 * k + 1], xyz3[3 * k + 2]);
+    const f3 vel = divs(sub(p, p), dt);
+    const uint32_t fl = (__float_as_uint(st[2 * v + 1].z) & FLAG_HAS_NORMAL) | FLAG_XO_IS_X;
+    st[2 * v] = make_float4(p.x, p.y, p.z, vel.x);
+    st[2 * v + 1] = make_float4(vel.y, vel.z, __uint_as_float(fl), 0.0f);
 }
 
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -338,10 +425,10 @@ cudaError_t launch_unpack_positions(const float4* state, int64_t n, float* out, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_state(const float4* state, const float4* normal, int64_t n, float* x, float* xo, float* nrm,
-                                cudaStream_t s) {
+cudaError_t launch_unpack_state(const float4* state, const float4* other, const float4* normal, int64_t n, float* x,
+                                float* xo, float* nrm, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_unpack_state<<<grid_for(n, 256), 256, 0, s>>>(state, normal, n, x, xo, nrm);
+    k_unpack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm);
     return cudaGetLastError();
 }
 
@@ -351,16 +438,16 @@ cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long 
     return cudaGetLastError();
 }
 
-cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, cudaStream_t s) {
+cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_set_vertices<<<grid_for(n, 256), 256, 0, s>>>(state, idx, xyz, n);
+    k_set_vertices<<<grid_for(n, 256), 256, 0, s>>>(state, idx, xyz, n, dt);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pack_state(float4* state, float4* normal, int64_t n, const float* x, const float* xo,
-                              const float* nrm, cudaStream_t s) {
+cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x, const float* xo,
+                              const float* nrm, float dt, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, normal, n, x, xo, nrm);
+    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm, dt);
     return cudaGetLastError();
 }
 
