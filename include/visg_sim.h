@@ -238,6 +238,42 @@ int visg_springs_from_mesh(const float* xyz, int32_t n_vertices,
                            uint32_t* row0, VisgSpring* ent0, int32_t* n_ent0,
                            uint32_t* row1, VisgSpring* ent1, int32_t* n_ent1);
 
+/* ======================================================================== */
+/* Body LBVH build that allocates no device memory.                           */
+/* ======================================================================== */
+/* No counterpart in the reference (its BVHAccel cudaMallocs in every build).
+ *
+ * For callers that cannot call cudaMalloc themselves or let a library do it: a
+ * host application whose own pool allocator owns the device memory, code running
+ * where an allocation would synchronise the device at the wrong moment, or a
+ * plugin that must not grow the process's memory after start-up.  The caller
+ * passes the body in device memory and the output arrays; every temporary of the
+ * build lives in one static device array of VISG_NOALLOC_SCRATCH_BYTES, reserved on
+ * every GPU that loads the library until the process exits.  The call makes no
+ * allocation of any kind.
+ *
+ *   d_xyz / d_normals   n_vertices*3 floats (normals may be NULL: no thickness push)
+ *   d_tris              n_tris*3 vertex indices, each < n_vertices (not checked)
+ *   outputs (device):   d_sorted_codes[n_tris], d_sorted_tris[n_tris] — the first T'
+ *                       entries are the de-duplicated Morton order;
+ *                       d_child_a/d_child_b[n_tris-1] — the first T'-1 entries are the
+ *                       radix tree's links in the reference's encoding (as
+ *                       visg_export_lbvh returns them); d_n_leaves[1] = T', or -1 if a
+ *                       bounded device wait gave up.
+ * Limits: n_vertices <= VISG_NOALLOC_MAX_VERTICES, n_tris <= VISG_NOALLOC_MAX_TRIS;
+ * larger bodies return VISG_ERR_INVALID_ARG.  Asynchronous on `cuda_stream`.  The
+ * first call on a device looks up the static array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
+ * share the array: calls whose GPU work overlaps (other streams, other threads) race. */
+#define VISG_NOALLOC_MAX_VERTICES 32768
+#define VISG_NOALLOC_MAX_TRIS 32768
+#define VISG_NOALLOC_SCRATCH_BYTES (9u * 1024u * 1024u)
+int visg_lbvh_build_noalloc(const float* d_xyz, const float* d_normals, int32_t n_vertices,
+                            const uint32_t* d_tris, int32_t n_tris, float thickness, float box_depth,
+                            uint32_t* d_sorted_codes, int32_t* d_sorted_tris,
+                            int32_t* d_child_a, int32_t* d_child_b, int32_t* d_n_leaves,
+                            void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,8 @@ def lib():
         "visg_batch_sync": (C.c_int, [_vp]),
         "visg_batch_destroy": (C.c_int, [_vp]),
         "visg_springs_from_mesh": (C.c_int, [_fp, C.c_int32, _u32p, C.c_int32, _u32p, _vp, _i32p, _u32p, _vp, _i32p]),
+        "visg_lbvh_build_noalloc": (C.c_int, [_vp, _vp, C.c_int32, _vp, C.c_int32, C.c_float, C.c_float, _vp, _vp,
+                                              _vp, _vp, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
