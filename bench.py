@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "fused_step_batched256.md")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "fused_step_batched.md")
 METRIC = "cloth vertex-steps/s"
 
 
@@ -319,7 +319,10 @@ def main():
     clocks = sampler.stop()
 
     # ---- roofline of the fused step kernel ---------------------------------------------
-    alg_bytes = 64 * nv + 4 * (nv + 1) + 8 * ne + 32 * contacts
+    # SURVEY 8(d) per-unit figure B_int = 72 N + 4 (N+1) L + s E with one merged row
+    # list (L = 1) and 8-byte entries (s = 8): x, x_old, normal read and written as
+    # 12-byte vectors, the row offset, and one entry per directed spring
+    alg_bytes = 72 * nv + 4 * (nv + 1) + 8 * ne
     t_launch = ms / 1e3 / args.steps
     achieved = alg_bytes / t_launch / 1e9
     peak, peak_kind = peak_hbm()
