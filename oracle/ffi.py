@@ -45,7 +45,7 @@ def lib():
         L.orc_sim_export_lbvh.argtypes = [C.c_void_p, _u32p, _fp, _u32p, _i32p, _i32p, _i32p, _i32p, _i32p,
                                           _fp, _fp, _fp]
         L.orc_sim_query.argtypes = [C.c_void_p, _fp, C.c_int, _i32p, _i32p, _dp, _dp]
-        L.orc_sim_forward.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        L.orc_sim_forward.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
         L.orc_sim_forward.restype = C.c_int
         L.orc_sim_backward.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_springs_from_mesh.argtypes = [_fp, C.c_int, _u32p, C.c_int, _u32p, C.c_void_p, _i32p,
@@ -170,9 +170,9 @@ class OracleSim:
         return leaf, inside, dist, nrm
 
     # adjoint (FP64 reference gradient when prec = 8)
-    def forward(self, nsteps: int):
+    def forward(self, nsteps: int, checkpoint_every: int = 50):
         rec = C.c_void_p()
-        lib().orc_sim_forward(self.h, nsteps, C.byref(rec))
+        lib().orc_sim_forward(self.h, nsteps, checkpoint_every, C.byref(rec))
         self._rec = rec
 
     def backward(self, dL_dx, dL_dxo=None):

@@ -441,57 +441,63 @@ struct Sim {
         r.hit.resize(N);
         for (int i = 0; i < N; ++i) r.hit[i] = (n[i].x != 0 || n[i].y != 0 || n[i].z != 0);
     }
+    // The reverse sweep runs in double whatever T is: with T = float it is the exact
+    // derivative of the float trajectory (per-step contributions of both signs cancel
+    // over many steps, which float accumulation would not resolve).
+    using D = double;
+    static V3<D> up(const V3<T>& v) { return mk<D>((D)v.x, (D)v.y, (D)v.z); }
     // Spring force derivative helper for entry i->j; returns the contributions of
     // adjoint G (of the force on i) to (x_i, xo_i, x_j, xo_j) and dF/dk, dF/dkd.
-    void spring_adj(const V3<T>& xi, const V3<T>& xoi, const V3<T>& xj, const V3<T>& xoj, T ks, T L0,
-                    const V3<T>& G, V3<T>& gxi, V3<T>& gxoi, V3<T>& gxj, V3<T>& gxoj, T& gk, T& gkd) const {
-        const T dt = (T)p.dt, kd = (T)p.spring_damping;
-        const T eps = (T)FLT_EPSILON_T;
-        V3<T> vi = (xi - xoi) / dt, vj = (xj - xoj) / dt;
-        V3<T> d = (xi - xj) + mk<T>(eps, eps, eps);
-        V3<T> dv = vi - vj;
-        T L = length(d);
-        V3<T> u = d / L;
-        T dvu = dot(dv, u);
-        T s = -ks * (L - L0) + kd * dvu;
-        T uG = dot(u, G);
+    void spring_adj(const V3<D>& xi, const V3<D>& xoi, const V3<D>& xj, const V3<D>& xoj, D ks, D L0,
+                    const V3<D>& G, V3<D>& gxi, V3<D>& gxoi, V3<D>& gxj, V3<D>& gxoj, D& gk, D& gkd) const {
+        const D dt = (D)p.dt, kd = (D)p.spring_damping;
+        const D eps = (D)FLT_EPSILON_T;
+        V3<D> vi = (xi - xoi) / dt, vj = (xj - xoj) / dt;
+        V3<D> d = (xi - xj) + mk<D>(eps, eps, eps);
+        V3<D> dv = vi - vj;
+        D L = length(d);
+        V3<D> u = d / L;
+        D dvu = dot(dv, u);
+        D s = -ks * (L - L0) + kd * dvu;
+        D uG = dot(u, G);
         // ds/dd = -ks u + kd/L (dv - dvu u); d(u)/dd = (I - u u^T)/L
-        V3<T> dsdd = (-ks) * u + (kd / L) * (dv - dvu * u);
-        V3<T> gd = uG * dsdd + (s / L) * (G - uG * u);
-        V3<T> gdv = (kd * uG) * u;
+        V3<D> dsdd = (-ks) * u + (kd / L) * (dv - dvu * u);
+        V3<D> gd = uG * dsdd + (s / L) * (G - uG * u);
+        V3<D> gdv = (kd * uG) * u;
         gxi = gd + gdv / dt;
-        gxoi = (T(-1) / dt) * gdv;
-        gxj = mk<T>(0, 0, 0) - gxi;
-        gxoj = mk<T>(0, 0, 0) - gxoi;
+        gxoi = (D(-1) / dt) * gdv;
+        gxj = mk<D>(0, 0, 0) - gxi;
+        gxoj = mk<D>(0, 0, 0) - gxoi;
         gk = -(L - L0) * uG;
         gkd = dvu * uG;
     }
     // Backward through one recorded step: lx, lxo are adjoints of the step's outputs
     // on entry and of its inputs on return.
-    void backward_step(const StepRec& r, std::vector<V3<T>>& lx, std::vector<V3<T>>& lxo,
+    void backward_step(const StepRec& r, std::vector<V3<D>>& lx, std::vector<V3<D>>& lxo,
                        std::vector<std::vector<double>>& dk, double& dgamma, double& dc, double& dkd) {
-        const T dt = (T)p.dt, mass = (T)p.mass, gamma = (T)p.verlet_damping;
-        std::vector<V3<T>> G(N), nlx(N, mk<T>(0, 0, 0)), nlxo(N, mk<T>(0, 0, 0));
+        const D dt = (D)p.dt, mass = (D)p.mass, gamma = (D)p.verlet_damping;
+        std::vector<V3<D>> G(N), nlx(N, mk<D>(0, 0, 0)), nlxo(N, mk<D>(0, 0, 0));
         for (int i = 0; i < N; ++i) {
-            if (pinned[i]) { nlx[i] = nlx[i] + lx[i] + lxo[i]; G[i] = mk<T>(0, 0, 0); continue; }
-            V3<T> lstar;
+            if (pinned[i]) { nlx[i] = nlx[i] + lx[i] + lxo[i]; G[i] = mk<D>(0, 0, 0); continue; }
+            V3<D> lstar;
             if (r.hit[i]) {
-                V3<T> a = lx[i] + lxo[i];
-                V3<T> nu = r.nu[i];
+                V3<D> a = lx[i] + lxo[i];
+                V3<D> nu = up(r.nu[i]);
                 lstar = a - dot(nu, a) * nu;
             } else {
                 lstar = lx[i];
                 nlx[i] = nlx[i] + lxo[i];
             }
-            nlx[i] = nlx[i] + (T(1) + gamma) * lstar;
+            const V3<D> xi = up(r.x[i]), xoi = up(r.xo[i]);
+            nlx[i] = nlx[i] + (D(1) + gamma) * lstar;
             nlxo[i] = nlxo[i] - gamma * lstar;
-            dgamma += (double)dot(lstar, r.x[i] - r.xo[i]);
-            V3<T> h = ((dt * dt) / mass) * lstar;
-            V3<T> np = r.nprev[i];
+            dgamma += dot(lstar, xi - xoi);
+            V3<D> h = ((dt * dt) / mass) * lstar;
+            V3<D> np = up(r.nprev[i]);
             G[i] = h - dot(np, h) * np;
-            V3<T> v = (r.x[i] - r.xo[i]) / dt;
-            dc += (double)dot(G[i], v);
-            T c = (T)p.force_damping;
+            V3<D> v = (xi - xoi) / dt;
+            dc += dot(G[i], v);
+            D c = (D)p.force_damping;
             nlx[i] = nlx[i] + (c / dt) * G[i];
             nlxo[i] = nlxo[i] - (c / dt) * G[i];
         }
@@ -500,17 +506,18 @@ struct Sim {
             for (size_t l = 0; l < lists.size(); ++l) {
                 const List& Ls = lists[l];
                 for (uint32_t e = Ls.row[i]; e < Ls.row[i + 1]; ++e) {
-                    T ks = Ls.k.empty() ? (T)p.list_k[l] : (T)Ls.k[e];
+                    D ks = Ls.k.empty() ? (D)p.list_k[l] : (D)Ls.k[e];
                     int j = Ls.ent[e].end;
-                    V3<T> gxi, gxoi, gxj, gxoj;
-                    T gk, gkd;
-                    spring_adj(r.x[i], r.xo[i], r.x[j], r.xo[j], ks, (T)Ls.ent[e].rest, G[i], gxi, gxoi, gxj, gxoj, gk, gkd);
+                    V3<D> gxi, gxoi, gxj, gxoj;
+                    D gk, gkd;
+                    spring_adj(up(r.x[i]), up(r.xo[i]), up(r.x[j]), up(r.xo[j]), ks, (D)Ls.ent[e].rest, G[i], gxi, gxoi,
+                               gxj, gxoj, gk, gkd);
                     nlx[i] = nlx[i] + gxi;
                     nlxo[i] = nlxo[i] + gxoi;
                     nlx[j] = nlx[j] + gxj;
                     nlxo[j] = nlxo[j] + gxoj;
-                    dk[l][e] += (double)gk;
-                    dkd += (double)gkd;
+                    dk[l][e] += gk;
+                    dkd += gkd;
                 }
             }
         }
@@ -689,38 +696,73 @@ void orc_sim_query(void* hv, const float* pts, int n, int32_t* leaf, int32_t* in
     });
 }
 
-// Forward with per-step records (adjoint).  Stores every step (the oracle is only run
-// at sizes where that fits); checkpoint_every is accepted for interface symmetry.
-int orc_sim_forward(void* hv, int nsteps, void** rec_out) {
+// Forward for the adjoint: the state (x, x_old, normal) every `ckpt` steps and at the
+// end; the backward pass replays each segment from its checkpoint (same results, so
+// the same contact set) and walks it in reverse.
+}  // extern "C"
+
+template <typename T>
+struct Tape {
+    int nsteps = 0, ckpt = 1;
+    std::vector<std::vector<V3<T>>> cx, cxo, cn;  // checkpoints
+    std::vector<V3<T>> fx, fxo, fn;               // final state
+};
+
+extern "C" {
+
+int orc_sim_forward(void* hv, int nsteps, int ckpt, void** tape_out) {
     ORC_DISPATCH(hv, {
         using TT = std::remove_reference_t<decltype(s->x[0][0].x)>;
-        auto* recs = new std::vector<typename Sim<TT>::StepRec>(nsteps);
-        for (int k = 0; k < nsteps; ++k) s->record_step((*recs)[k]);
-        *rec_out = recs;
+        auto* tp = new Tape<TT>();
+        tp->nsteps = nsteps;
+        tp->ckpt = ckpt < 1 ? 1 : ckpt;
+        for (int k = 0; k < nsteps; ++k) {
+            if (k % tp->ckpt == 0) {
+                tp->cx.push_back(s->x[s->cur]);
+                tp->cxo.push_back(s->xo[s->cur]);
+                tp->cn.push_back(s->n);
+            }
+            s->step();
+        }
+        tp->fx = s->x[s->cur];
+        tp->fxo = s->xo[s->cur];
+        tp->fn = s->n;
+        *tape_out = tp;
     });
     return 0;
 }
 
-void orc_sim_backward(void* hv, void* recv, const double* dL_dx, const double* dL_dxo, double* dk_out,
+void orc_sim_backward(void* hv, void* tape, const double* dL_dx, const double* dL_dxo, double* dk_out,
                       double* dscalar) {
     ORC_DISPATCH(hv, {
         using TT = std::remove_reference_t<decltype(s->x[0][0].x)>;
-        auto* recs = (std::vector<typename Sim<TT>::StepRec>*)recv;
-        std::vector<V3<TT>> lx(s->N), lxo(s->N);
+        auto* tp = (Tape<TT>*)tape;
+        std::vector<V3<double>> lx(s->N), lxo(s->N);
         for (int i = 0; i < s->N; ++i) {
-            lx[i] = mk<TT>((TT)dL_dx[3 * i], (TT)dL_dx[3 * i + 1], (TT)dL_dx[3 * i + 2]);
-            lxo[i] = dL_dxo ? mk<TT>((TT)dL_dxo[3 * i], (TT)dL_dxo[3 * i + 1], (TT)dL_dxo[3 * i + 2])
-                            : mk<TT>(0, 0, 0);
+            lx[i] = mk<double>(dL_dx[3 * i], dL_dx[3 * i + 1], dL_dx[3 * i + 2]);
+            lxo[i] = dL_dxo ? mk<double>(dL_dxo[3 * i], dL_dxo[3 * i + 1], dL_dxo[3 * i + 2]) : mk<double>(0, 0, 0);
         }
         std::vector<std::vector<double>> dk(s->lists.size());
         for (size_t l = 0; l < s->lists.size(); ++l) dk[l].assign(s->lists[l].ent.size(), 0.0);
         double dg = 0, dc = 0, dkd = 0;
-        for (int k = (int)recs->size() - 1; k >= 0; --k) s->backward_step((*recs)[k], lx, lxo, dk, dg, dc, dkd);
+        const int nseg = (int)tp->cx.size();
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int s0 = seg * tp->ckpt, s1 = std::min(s0 + tp->ckpt, tp->nsteps);
+            s->x[s->cur] = tp->cx[seg];
+            s->xo[s->cur] = tp->cxo[seg];
+            s->n = tp->cn[seg];
+            std::vector<typename Sim<TT>::StepRec> recs(s1 - s0);
+            for (int k = 0; k < s1 - s0; ++k) s->record_step(recs[k]);
+            for (int k = s1 - s0 - 1; k >= 0; --k) s->backward_step(recs[k], lx, lxo, dk, dg, dc, dkd);
+        }
+        s->x[s->cur] = tp->fx;
+        s->xo[s->cur] = tp->fxo;
+        s->n = tp->fn;
         size_t off = 0;
         for (size_t l = 0; l < dk.size(); ++l)
             for (size_t e = 0; e < dk[l].size(); ++e) dk_out[off++] = dk[l][e];
         dscalar[0] = dg; dscalar[1] = dc; dscalar[2] = dkd;
-        delete recs;
+        delete tp;
     });
 }
 

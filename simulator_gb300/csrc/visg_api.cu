@@ -127,18 +127,15 @@ struct Engine {
     int sm_count = 0;
     // adjoint records
     struct Adj {
-        int ckpt_every = 0, nsteps = 0;
-        std::vector<float4*> ck_state;  // checkpoints (2N float4 each)
-        std::vector<float4*> ck_normal;
-        float4* seg_state = nullptr;    // ckpt_every+1 states of the segment being replayed
-        float4* seg_hit = nullptr;      // ckpt_every hit records
-        float4* seg_nin = nullptr;      // ckpt_every normals entering each step
-        float4* lam[2] = {nullptr, nullptr};
-        float4* G = nullptr;
-        float* dk = nullptr;
-        double* dsc = nullptr;
-        uint32_t* rev = nullptr;
-        int start_cur = 0;
+        int ckpt = 0, nsteps = 0;
+        std::vector<double*> ck;     // FP64 checkpoints: x, x_old, normal (9N doubles) every ckpt steps
+        double* s64 = nullptr;       // FP64 state: [x0 | xo0 | x1 | xo1 | n] (15N doubles)
+        double* rec = nullptr;       // (ckpt + 1) recorded states of the segment being replayed
+        double* lam = nullptr;       // 4 x 3N: adjoints of x, x_old (in / out)
+        double* G = nullptr;         // 3N
+        double* dk = nullptr;        // per merged entry
+        double* dsc = nullptr;       // 3
+        uint32_t* rev = nullptr;     // reverse entry of every merged entry
         bool ready = false;
     } adj;
 
@@ -169,11 +166,9 @@ struct Engine {
     }
 
     void free_adjoint() {
-        for (auto* q : adj.ck_state) cudaFree(q);
-        for (auto* q : adj.ck_normal) cudaFree(q);
-        adj.ck_state.clear();
-        adj.ck_normal.clear();
-        void* ps[] = {adj.seg_state, adj.seg_hit, adj.seg_nin, adj.lam[0], adj.lam[1], adj.G, adj.dk, adj.dsc, adj.rev};
+        for (auto* q : adj.ck) cudaFree(q);
+        adj.ck.clear();
+        void* ps[] = {adj.s64, adj.rec, adj.lam, adj.G, adj.dk, adj.dsc, adj.rev};
         for (void* q : ps)
             if (q) cudaFree(q);
         adj = Adj();
@@ -823,6 +818,9 @@ struct Engine {
 
     int forward(int nsteps, int ckpt);
     int backward(const float* dL_dx, const float* dL_dxo, float* dL_dk, float* dL_dscalar);
+    cudaError_t step64(int c);
+    cudaError_t save64(int c, double* dst);
+    cudaError_t load64(const double* src);
 };
 
 struct VisgSim {

@@ -159,26 +159,36 @@ cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long 
 cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt,
                                 cudaStream_t s);
 
-// ---- adjoint ---------------------------------------------------------------------------
+// ---- adjoint ----------------------------------------------------------------------------
+// Packed float3 arrays of one recorded step: x, x_old and the contact normal entering
+// the step (n_in), and the contact normals the step produced (n_out: non-zero = the
+// vertex was projected, with that plane normal).
 struct AdjArgs {
-    const float4* state;    // the step's input state (x, x_old, flags)
-    const float4* normal_in;  // contact normals entering the step (frozen projection)
-    const float4* hit;      // per vertex: projection normal of this step (w = 1 if projected)
+    const double* x;
+    const double* xo;
+    const double* n_in;
+    const double* n_out;
     const uint32_t* rowp;
     const uint2* ent;
-    const float* kent;
-    const uint32_t* rev;    // reverse entry of every directed spring
-    const float4* lam_in;   // 2 per vertex: adjoint of (x', x_old') of the step's outputs
-    float4* lam_out;        // 2 per vertex: adjoint of (x, x_old)
-    float4* G;              // per vertex: adjoint of the force
-    float* dk;              // per entry, accumulated
-    double* dscalar;        // [3] accumulated (gamma, force damping, kd)
+    const float* kent;     // per entry stiffness, or NULL (list stiffness)
+    const uint32_t* rev;   // reverse entry of every directed spring
+    const double* lx_in;   // adjoint of the step's outputs x', x_old' (double3 per vertex)
+    const double* lxo_in;
+    double* lx_out;        // adjoint of the step's inputs x, x_old
+    double* lxo_out;
+    double* G;             // adjoint of the force on each vertex (double3)
+    double* dk;            // per entry, accumulated over steps
+    double* dscalar;       // [3]: gamma, force damping, spring damping; accumulated
     int n;
     StepParams p;
 };
 cudaError_t launch_adjoint_step(const AdjArgs& a, cudaStream_t s);
-// forward step that also records, per vertex, the projection normal (w = 1 when projected)
-cudaError_t launch_record_hits(const float4* state_out, const float4* normal, int64_t n, float4* hit,
-                               cudaStream_t s);
+// the differentiable forward: one step in double (packed double3 arrays)
+cudaError_t launch_step_f64(const double* x, const double* xo, double* xn, double* xon, double* nrm,
+                            const uint32_t* rowp, const uint2* ent, const float* kent, const BvhView* bodies,
+                            const float4* body_verts, const uint32_t* body_tris, const StepParams& p, int refv,
+                            int collide, int n, int* err, cudaStream_t s);
+cudaError_t launch_widen(const float* src, double* dst, int64_t n, cudaStream_t s);
+cudaError_t launch_narrow(const double* src, float* dst, int64_t n, cudaStream_t s);
 
 }  // namespace visg
