@@ -62,6 +62,9 @@ typedef struct VisgParams {
     int32_t check_every;   /* every K steps check for NaN/Inf and |dx| > max_displacement; 0=off */
     float max_displacement;/* limit for the divergence check (metres per step)                  */
     int32_t use_graph;     /* 1: replay multi-step loops as CUDA graphs (default), 0: launches  */
+    int32_t split_collision; /* 1: collision in its own kernel over the vertices inside a body's
+                                box (default), 0: fused into the step kernel; same results.
+                                visg_batch_autotune may change it.                             */
 } VisgParams;
 
 void visg_default_params(VisgParams* p);

@@ -116,6 +116,9 @@ struct Engine {
     std::vector<BvhBuffers> bvh;
     int* d_err = nullptr;
     uint32_t* d_check = nullptr;
+    int2* d_cand = nullptr;            // split collision: queued candidates
+    uint32_t* d_cand_count = nullptr;
+    int split = 1;                     // collision in its own kernel (autotuned)
     float* d_stage = nullptr;  // 9*N floats
     uint32_t* h_status = nullptr;  // pinned: err, check0, check1
     int cur = 0;
@@ -223,6 +226,7 @@ struct Engine {
     }
 
     int finalize() {
+        split = p.split_collision ? 1 : 0;
         if (finalized) return fail(VISG_ERR_STATE, "already finalized");
         if (gin.empty()) return fail(VISG_ERR_INVALID_ARG, "no garments");
         int dev = 0;
@@ -293,6 +297,8 @@ struct Engine {
         arena.want(&d_views, (size_t)G);
         arena.want(&d_err, 4);
         arena.want(&d_check, 4);
+        arena.want(&d_cand, (size_t)N + 1);
+        arena.want(&d_cand_count, 4);
         arena.want(&d_stage, 9 * (size_t)N + 4);
         bvh.resize(G);
         for (int g = 0; g < G; ++g)
@@ -345,6 +351,7 @@ struct Engine {
         if (perk) v |= SV_PERK;
         if (p.verlet_damping == 1.0f) v |= SV_REFV;
         if (p.collide && any_body) v |= SV_COLLIDE;
+        if (p.collide && any_body && split) v |= SV_SPLIT;
         if (p.check_every > 0) v |= SV_CHECK;
         uint32_t kdbits;
         std::memcpy(&kdbits, &p.spring_damping, 4);
@@ -382,6 +389,8 @@ struct Engine {
         a.bodies = d_views;
         a.err = d_err;
         a.check = d_check;
+        a.cand = d_cand;
+        a.cand_count = d_cand_count;
         a.p = step_params();
         return a;
     }
@@ -762,8 +771,12 @@ struct Engine {
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         float best = 1e30f;
-        int best_block = block, best_grid = grid, best_ctas = 0;
-        for (int bi = 0; bi < 3 && e == cudaSuccess; ++bi) {
+        int best_block = block, best_grid = grid, best_ctas = 0, best_split = split;
+        const int split0 = split;
+        const int n_split = (p.collide && any_body) ? 2 : 1;
+        for (int sv = 0; sv < n_split * 3 && e == cudaSuccess; ++sv) {
+            split = sv / 3;
+            const int bi = sv % 3;
             const int blk = kBlocks[bi];
             const int occ = step_max_ctas_per_sm(variant(), blk);
             std::vector<int> ctas;
@@ -790,9 +803,11 @@ struct Engine {
                     best_block = blk;
                     best_grid = gr;
                     best_ctas = c;
+                    best_split = split;
                 }
             }
         }
+        split = split0;
         cur = cur0;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(d_state[cur], bs, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
@@ -806,9 +821,10 @@ struct Engine {
         cudaFree(bs);
         cudaFree(bn);
         if (e != cudaSuccess) return cuda_fail(e, "autotune");
-        if (best_block != block || best_grid != grid) {
+        if (best_block != block || best_grid != grid || best_split != split) {
             block = best_block;
             grid = best_grid;
+            split = best_split;
             destroy_graphs();
         }
         if (out_block) *out_block = block;
@@ -857,6 +873,7 @@ void visg_default_params(VisgParams* p) {
     p->check_every = 0;
     p->max_displacement = 1.0f;
     p->use_graph = 1;
+    p->split_collision = 1;
 }
 
 const char* visg_version(void) { return "visg-gb300 1.0 (sm_103a)"; }

@@ -127,6 +127,8 @@ struct StepArgs {
     const BvhView* bodies;  // per garment
     int* err;
     uint32_t* check;  // [0] max |dx| bits, [1] non-finite count
+    int2* cand;       // split collision: {vertex, garment} of the vertices inside their body's box
+    uint32_t* cand_count;
     StepParams p;
 };
 
@@ -136,6 +138,7 @@ enum StepVariant : int {
     SV_COLLIDE = 4,   // body collision
     SV_CHECK = 8,     // divergence check
     SV_KD0 = 16,      // spring damping exactly +0
+    SV_SPLIT = 32,    // collision in its own kernel over a compacted candidate list
 };
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
 int step_max_ctas_per_sm(int variant, int block);

@@ -166,7 +166,7 @@ __device__ __forceinline__ f3 spring_sum(const StepArgs& a, const float4* __rest
 // v = (x - x_old) / dt.  x_old is x itself when FLAG_XO_IS_X is set (after a
 // contact, a pin or update_vertex) and otherwise the previous step's x, which is
 // still in the other buffer: the step reads it there before overwriting it.
-template <int BLOCK, bool COLL, bool KD0>
+template <int BLOCK, bool COLL, bool KD0, bool SPLIT>
 __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
     const StepParams& P = a.p;
     const f3 grav = mk3(P.gx, P.gy, P.gz);
@@ -202,7 +202,22 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
             else xn = add(add(x, mul(P.gamma, sub(x, xo))), adt);
             xon = x;
         }
-        if (COLL) {
+        if (COLL && SPLIT) {
+            // split collision: queue the vertices inside their body's box (one atomic per
+            // warp); k_collide traverses them with fully populated warps
+            const BvhView bv = a.bodies[td.x];
+            bool cand = false;
+            if (bv.root != nullptr)
+                cand = active && !pinned && bv.root->n_leaves > 0 && in_box(xn, bv.root->top_lo, bv.root->top_hi);
+            const unsigned m = __ballot_sync(0xffffffffu, cand);
+            if (m) {
+                const int lane = (int)(threadIdx.x & 31u), leader = __ffs(m) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(a.cand_count, (uint32_t)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (cand) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, td.x);
+            }
+        } else if (COLL) {
             const BvhView bv = a.bodies[td.x];
             if (bv.root != nullptr) {
                 const int nl = bv.root->n_leaves;
@@ -259,10 +274,58 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
     }
 }
 
+// Split collision (collision_response_projection, verlet.cu:24-50) over the queued
+// candidates: the integrate pass has already written every vertex's record as if
+// it had no contact; a projected vertex gets x' += |dist| n, x_old' = x', v' = 0
+// and its normal.
+constexpr int COLLIDE_BLOCK = 256;
+__global__ void __launch_bounds__(COLLIDE_BLOCK) k_collide(const StepArgs a) {
+    const uint32_t n = *a.cand_count;
+    const float dt = a.p.dt;
+    for (uint32_t k = blockIdx.x * COLLIDE_BLOCK + threadIdx.x; k < n; k += gridDim.x * COLLIDE_BLOCK) {
+        const int2 c = a.cand[k];
+        const BvhView bv = a.bodies[c.y];
+        const int nl = bv.root->n_leaves;
+        const float4 s0 = a.state_out[2 * c.x];
+        f3 xn = mk3(s0.x, s0.y, s0.z);
+        const int leaf = nl == 1 ? 0 : first_hit(bv.nodes, bv.root->root, nl, xn, a.err);
+        if (leaf < 0) continue;
+        const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
+        const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
+        const f3 nrm = mk3(L0.w, L1.x, L1.y);
+        const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), nrm);
+        if (d > 0.0f) continue;
+        xn = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), nrm));
+        const f3 vn = divs(sub(xn, xn), dt);
+        a.state_out[2 * c.x] = make_float4(xn.x, xn.y, xn.z, vn.x);
+        a.state_out[2 * c.x + 1] =
+            make_float4(vn.y, vn.z, __uint_as_float(FLAG_HAS_NORMAL | FLAG_XO_IS_X), 0.0f);
+        a.normal[c.x] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+    }
+}
+
+int g_collide_grid = 0;
+
 template <int BLOCK, bool KD0>
-cudaError_t launch_kd(const StepArgs& a, bool coll, int refv, int check, int perk, int grid, cudaStream_t s) {
-    if (coll) k_step<BLOCK, true, KD0><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
-    else k_step<BLOCK, false, KD0><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
+cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int check, int perk, int grid,
+                      cudaStream_t s) {
+    if (coll && split) {
+        cudaError_t e = cudaMemsetAsync(a.cand_count, 0, sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
+        k_step<BLOCK, true, KD0, true><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
+        if (g_collide_grid == 0) {
+            int dev = 0, sms = 0, occ = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_collide, COLLIDE_BLOCK, 0);
+            g_collide_grid = sms * (occ > 0 ? occ : 1);
+        }
+        k_collide<<<g_collide_grid, COLLIDE_BLOCK, 0, s>>>(a);
+    } else if (coll) {
+        k_step<BLOCK, true, KD0, false><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
+    } else {
+        k_step<BLOCK, false, KD0, false><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
+    }
     return cudaGetLastError();
 }
 
@@ -271,23 +334,24 @@ cudaError_t launch_block(const StepArgs& a, int variant, int grid, cudaStream_t 
     const int refv = (variant & SV_REFV) ? 1 : 0;
     const int check = (variant & SV_CHECK) ? 1 : 0;
     const int perk = (variant & SV_PERK) ? 1 : 0;
-    const bool coll = (variant & SV_COLLIDE) != 0;
-    if (variant & SV_KD0) return launch_kd<BLOCK, true>(a, coll, refv, check, perk, grid, s);
-    return launch_kd<BLOCK, false>(a, coll, refv, check, perk, grid, s);
+    const bool coll = (variant & SV_COLLIDE) != 0, split = (variant & SV_SPLIT) != 0;
+    if (variant & SV_KD0) return launch_kd<BLOCK, true>(a, coll, split, refv, check, perk, grid, s);
+    return launch_kd<BLOCK, false>(a, coll, split, refv, check, perk, grid, s);
 }
 
 template <int BLOCK, bool KD0>
-int occupancy_kd(bool coll) {
+int occupancy_kd(bool coll, bool split) {
     int n = 0;
-    if (coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, KD0>, BLOCK, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, KD0>, BLOCK, 0);
+    if (coll && split) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, KD0, true>, BLOCK, 0);
+    else if (coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, KD0, false>, BLOCK, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, KD0, false>, BLOCK, 0);
     return n;
 }
 
 template <int BLOCK>
 int occupancy_block(int variant) {
-    const bool coll = (variant & SV_COLLIDE) != 0;
-    return (variant & SV_KD0) ? occupancy_kd<BLOCK, true>(coll) : occupancy_kd<BLOCK, false>(coll);
+    const bool coll = (variant & SV_COLLIDE) != 0, split = (variant & SV_SPLIT) != 0;
+    return (variant & SV_KD0) ? occupancy_kd<BLOCK, true>(coll, split) : occupancy_kd<BLOCK, false>(coll, split);
 }
 
 __global__ void k_query(BvhView bv, const float* __restrict__ pts, int n, int* leaf, int* inside, float* dist,

@@ -7,6 +7,7 @@ tests/golden/make_golden.py and their outputs committed here.  The CPU oracle mu
 reproduce them bit for bit: the LBVH of three bodies and a 200-step trajectory
 with contacts.  This pins the oracle that the GPU tests compare the library with.
 """
+import ctypes as C
 import glob
 import os
 
@@ -44,7 +45,9 @@ def test_oracle_lbvh_matches_reference_kernels(path):
 @pytest.mark.parametrize("path", TRAJ, ids=[os.path.basename(p) for p in TRAJ])
 def test_oracle_trajectory_matches_reference_kernels(path):
     g = np.load(path)
-    p = VisgParams.from_buffer_copy(g["params"].tobytes())
+    raw = g["params"].tobytes()  # the struct as written; fields added later are appended (zero)
+    raw = raw + bytes(max(0, C.sizeof(VisgParams) - len(raw)))
+    p = VisgParams.from_buffer_copy(raw[: C.sizeof(VisgParams)])
     lists = []
     for l in (0, 1):
         ent = np.zeros(len(g[f"end{l}"]), scenes.SPRING_DTYPE)

@@ -206,6 +206,22 @@ def test_graph_replay_equals_single_launches():
         assert np.array_equal(u, v)
 
 
+@pytest.mark.parametrize("lists", ["grid", "mesh"])
+def test_split_and_fused_collision_identical(lists):
+    cloth, cl, body, p = ref_scene(side=32, subdiv=3, lists=lists)
+    pf = reference_params(len(cl))
+    for f, _ in vs.VisgParams._fields_:
+        setattr(pf, f, getattr(p, f))
+    pf.split_collision = 0
+    a = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    b = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=pf)
+    a.simulate(150)
+    b.simulate(150)
+    for u, v in zip(a.state(), b.state()):
+        assert np.array_equal(u, v)
+    assert a.count_contacts() > 10
+
+
 def test_set_vertex_and_state_roundtrip():
     cloth, cl, body, p = ref_scene(side=16, subdiv=2)
     g = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
