@@ -65,6 +65,13 @@ typedef struct VisgParams {
     int32_t split_collision; /* 1: collision in its own kernel over the vertices inside a body's
                                 box (default), 0: fused into the step kernel; same results.
                                 visg_batch_autotune may change it.                             */
+    int32_t stage_neighbours; /* 1: each tile's window of neighbour records is staged in shared
+                                memory by TMA bulk copies (default), 0: read from global memory;
+                                same results.  visg_batch_autotune may change it.              */
+    int32_t collision_margin; /* 1: each vertex keeps a proven lower bound of its distance to
+                                every leaf box of its body and skips the first-hit query
+                                while it has moved less than that (default); 0: query every
+                                step.  Same results; update_body clears the bounds.        */
 } VisgParams;
 
 void visg_default_params(VisgParams* p);
@@ -135,6 +142,17 @@ int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n);
  * device pointer and the copy is asynchronous; 0: host pointer (pinned or pageable),
  * synchronises and reports any device-side error (divergence, timeout). */
 int visg_get_positions(VisgSim* sim, float* out, int32_t on_device);
+
+/* Pipelined read-back (no counterpart in the reference, whose cuda_update_vbo
+ * copies synchronously every frame): enqueues, behind the steps issued so far, the
+ * copy of all n_vertices*3 positions into host memory `out` (page-locked memory
+ * lets the copy run asynchronously) and returns at once, so the steps issued next
+ * run while the copy proceeds.  At most two reads may be in flight; `out` must
+ * stay valid until visg_wait_positions has returned for it.  visg_wait_positions
+ * waits for the oldest read in flight and reports device-side errors raised up to
+ * the step it read. */
+int visg_read_positions_async(VisgSim* sim, float* out);
+int visg_wait_positions(VisgSim* sim);
 
 /* Full step state (x, x_old, previous contact normal; n_vertices*3 floats each, host).
  * Any pointer may be NULL.  get synchronises. */
@@ -211,6 +229,9 @@ int visg_batch_set_stream(VisgBatch* b, void* cuda_stream);
 int visg_batch_step(VisgBatch* b, int32_t nsteps);
 /* garment = -1: all garments concatenated in id order. */
 int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device);
+/* visg_read_positions_async / visg_wait_positions over all garments (concatenated). */
+int visg_batch_read_positions_async(VisgBatch* b, float* out);
+int visg_batch_wait_positions(VisgBatch* b);
 int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]);
 /* visg_set_vertices over the whole batch: idx are global vertex indices (garments
  * concatenated in id order). */
@@ -221,6 +242,11 @@ int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* body_xyz,
  * and keeps the fastest; *block and *ctas_per_sm (may be NULL) report the choice.
  * Leaves the simulation state unchanged. */
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm);
+/* Sets the step kernel's launch shape directly (no timing): block = 128, 256 or
+ * 512 vertices per tile; ctas_per_sm = persistent CTAs per SM (1 .. what fits), or
+ * 0 for one CTA per tile.  For reproducible timings and for callers that tune
+ * offline.  No counterpart in the reference (it launches one fixed shape). */
+int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas_per_sm);
 int visg_batch_info(VisgBatch* b, int32_t* n_garments, int64_t* n_vertices,
                     int64_t* n_entries, int64_t* n_tris);
 int visg_batch_count_contacts(VisgBatch* b, int64_t* n);

@@ -84,6 +84,11 @@ def lib():
         "visg_batch_set_vertex": (C.c_int, [_vp, C.c_int32, C.c_uint32, _fp]),
         "visg_batch_update_body": (C.c_int, [_vp, C.c_int32, _fp, _fp]),
         "visg_batch_autotune": (C.c_int, [_vp, _i32p, _i32p]),
+        "visg_batch_set_launch": (C.c_int, [_vp, C.c_int32, C.c_int32]),
+        "visg_batch_read_positions_async": (C.c_int, [_vp, _vp]),
+        "visg_batch_wait_positions": (C.c_int, [_vp]),
+        "visg_read_positions_async": (C.c_int, [_vp, _vp]),
+        "visg_wait_positions": (C.c_int, [_vp]),
         "visg_batch_info": (C.c_int, [_vp, _i32p, _i64p, _i64p, _i64p]),
         "visg_batch_sync": (C.c_int, [_vp]),
         "visg_batch_destroy": (C.c_int, [_vp]),
@@ -207,6 +212,16 @@ class Simulator:
     def positions_device(self, dev_ptr: int):
         _check(lib().visg_get_positions(self.h, dev_ptr, 1))
 
+    def read_positions_async(self, out):
+        """Enqueue the read of all positions into `out` ((n, 3) float32, ideally
+        page-locked) behind the steps issued so far; returns at once."""
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 3 * self.n
+        _check(lib().visg_read_positions_async(self.h, out.ctypes.data))
+
+    def wait_positions(self):
+        """Wait for the oldest read in flight."""
+        _check(lib().visg_wait_positions(self.h))
+
     def state(self):
         x, xo, n = (np.empty((self.n, 3), np.float32) for _ in range(3))
         _check(lib().visg_get_state(self.h, _p(x), _p(xo), _p(n)))
@@ -311,6 +326,16 @@ class BatchSimulator:
     def positions_device(self, dev_ptr: int, garment: int = -1):
         _check(lib().visg_batch_get_positions(self.h, garment, dev_ptr, 1))
 
+    def read_positions_async(self, out):
+        """Enqueue the read of every garment's positions (concatenated) into `out`
+        ((n, 3) float32, ideally page-locked) behind the steps issued so far."""
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 3 * int(self.offsets[-1])
+        _check(lib().visg_batch_read_positions_async(self.h, out.ctypes.data))
+
+    def wait_positions(self):
+        """Wait for the oldest read in flight."""
+        _check(lib().visg_batch_wait_positions(self.h))
+
     def update_vertex(self, garment: int, new_value, idx: int):
         v = _f32(new_value).reshape(3)
         _check(lib().visg_batch_set_vertex(self.h, garment, idx, _p(v)))
@@ -328,6 +353,9 @@ class BatchSimulator:
         b, c = C.c_int32(), C.c_int32()
         _check(lib().visg_batch_autotune(self.h, C.byref(b), C.byref(c)))
         return b.value, c.value
+
+    def set_launch(self, block: int, ctas_per_sm: int):
+        _check(lib().visg_batch_set_launch(self.h, block, ctas_per_sm))
 
     def info(self):
         g = C.c_int32()

@@ -39,6 +39,9 @@ int cuda_fail(cudaError_t e, const char* what) {
     } while (0)
 
 constexpr int kBlocks[3] = {128, 256, 512};
+// largest neighbour window (vertex records) a tile of each block size may stage:
+// two buffers of it stay within 64 / 96 / 128 KB of shared memory
+constexpr int kWindowCap[3] = {1024, 1536, 2048};
 int block_index(int b) { return b == 128 ? 0 : (b == 256 ? 1 : (b == 512 ? 2 : -1)); }
 
 struct GarmentIn {
@@ -112,6 +115,14 @@ struct Engine {
     float* d_k = nullptr;
     int4* d_tiles[3] = {nullptr, nullptr, nullptr};
     int n_tiles[3] = {0, 0, 0};
+    int2* d_twin[3] = {nullptr, nullptr, nullptr};  // per tile neighbour window (staged step)
+    int win_cap[3] = {0, 0, 0};                      // records per stage buffer, 0 = no tile staged
+    uint2* d_sell = nullptr;                         // sliced-ELL springs
+    float* d_sellk = nullptr;
+    uint32_t* d_slice_off = nullptr;
+    uint32_t* d_vinfo = nullptr;
+    std::vector<uint32_t> h_vinfo;                   // row length | pin bit, per vertex
+    int stage = 1;                                   // stage neighbour windows (autotuned)
     BvhView* d_views = nullptr;
     std::vector<BvhBuffers> bvh;
     int* d_err = nullptr;
@@ -142,9 +153,28 @@ struct Engine {
         bool ready = false;
     } adj;
 
+    // asynchronous position read-back: two device staging slots copied to host memory
+    // on their own stream while later steps run
+    struct Readback {
+        cudaStream_t copy = nullptr;
+        float* d_pos[2] = {nullptr, nullptr};
+        cudaEvent_t unpacked[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+        uint32_t* h_err = nullptr;  // pinned: the error word as of each slot's read
+        bool used[2] = {false, false};
+        int next = 0;     // slot of the next read
+        int pending = 0;  // reads issued and not yet waited for (0..2)
+    } rb;
+
     ~Engine() {
         if (stream) cudaStreamSynchronize(stream);
         cudaDeviceSynchronize();
+        for (int k = 0; k < 2; ++k) {
+            if (rb.d_pos[k]) cudaFree(rb.d_pos[k]);
+            if (rb.unpacked[k]) cudaEventDestroy(rb.unpacked[k]);
+            if (rb.copied[k]) cudaEventDestroy(rb.copied[k]);
+        }
+        if (rb.copy) cudaStreamDestroy(rb.copy);
+        if (rb.h_err) cudaFreeHost(rb.h_err);
         destroy_graphs();
         if (d_sv_idx) cudaFree(d_sv_idx);
         if (h_sv) cudaFreeHost(h_sv);
@@ -227,6 +257,7 @@ struct Engine {
 
     int finalize() {
         split = p.split_collision ? 1 : 0;
+        stage = p.stage_neighbours ? 1 : 0;
         if (finalized) return fail(VISG_ERR_STATE, "already finalized");
         if (gin.empty()) return fail(VISG_ERR_INVALID_ARG, "no garments");
         int dev = 0;
@@ -277,12 +308,68 @@ struct Engine {
             for (uint32_t v : gi.pinned) h_rowp[voff[g] + v] |= PIN_BIT;
         }
         h_rowp[N] = (uint32_t)E;
-        // tiles for each block size
-        std::vector<std::vector<int4>> tiles(3);
-        for (int b = 0; b < 3; ++b)
+        // sliced ELL: slices of 32 vertices of one garment, each padded to its longest row
+        std::vector<int64_t> slice0(G + 1, 0);
+        for (int g = 0; g < G; ++g) slice0[g + 1] = slice0[g] + (gin[g].N + 31) / 32;
+        const int64_t S = slice0[G];
+        std::vector<uint32_t> soff(S + 1, 0);
+        std::vector<uint32_t>& vinfo = h_vinfo;
+        vinfo.assign(N, 0u);
+        auto row_len = [&](int64_t v) { return (h_rowp[v + 1] & ROW_MASK) - (h_rowp[v] & ROW_MASK); };
+        {
+            uint64_t c2 = 0;
             for (int g = 0; g < G; ++g)
-                for (int64_t v = voff[g]; v < voff[g + 1]; v += kBlocks[b])
-                    tiles[b].push_back(make_int4(g, (int)v, (int)std::min<int64_t>(v + kBlocks[b], voff[g + 1]), 0));
+                for (int64_t s = slice0[g]; s < slice0[g + 1]; ++s) {
+                    const int64_t v0 = voff[g] + 32 * (s - slice0[g]), v1 = std::min<int64_t>(v0 + 32, voff[g + 1]);
+                    uint32_t w = 0;
+                    for (int64_t v = v0; v < v1; ++v) w = std::max(w, row_len(v));
+                    soff[s] = (uint32_t)c2;
+                    c2 += 32ull * w;
+                    if (c2 >= 0xffffffffull) return fail(VISG_ERR_INVALID_ARG, "too many spring entries");
+                }
+            soff[S] = (uint32_t)c2;
+        }
+        const int64_t ES = soff[S];
+        std::vector<uint2> sell(ES > 0 ? ES : 1, make_uint2(0u, 0u));
+        std::vector<float> sellk;
+        if (perk) sellk.assign(ES > 0 ? ES : 1, 0.0f);
+        for (int g = 0; g < G; ++g)
+            for (int64_t v = voff[g]; v < voff[g + 1]; ++v) {
+                const int64_t s = slice0[g] + (v - voff[g]) / 32;
+                const int64_t lane = (v - voff[g]) % 32;
+                const uint32_t rp = h_rowp[v] & ROW_MASK, n = row_len(v);
+                vinfo[v] = n | (h_rowp[v] & PIN_BIT);
+                for (uint32_t k = 0; k < n; ++k) {
+                    sell[soff[s] + 32 * (int64_t)k + lane] = ent[rp + k];
+                    if (perk) sellk[soff[s] + 32 * (int64_t)k + lane] = kk[rp + k];
+                }
+            }
+        // tiles for each block size, with the window of vertex records each one's springs touch
+        std::vector<std::vector<int4>> tiles(3);
+        std::vector<std::vector<int2>> twin(3);
+        for (int b = 0; b < 3; ++b) {
+            const int cap = kWindowCap[b];
+            win_cap[b] = 0;
+            for (int g = 0; g < G; ++g)
+                for (int64_t v = voff[g]; v < voff[g + 1]; v += kBlocks[b]) {
+                    const int64_t v1 = std::min<int64_t>(v + kBlocks[b], voff[g + 1]);
+                    tiles[b].push_back(make_int4(g, (int)v, (int)v1, (int)(slice0[g] + (v - voff[g]) / 32)));
+                    int64_t lo = v, hi = v1;
+                    for (int64_t u = v; u < v1; ++u)
+                        for (uint32_t e = h_rowp[u] & ROW_MASK; e < (h_rowp[u + 1] & ROW_MASK); ++e) {
+                            const int64_t j = ent[e].x & END_MASK;
+                            lo = std::min(lo, j);
+                            hi = std::max(hi, j + 1);
+                        }
+                    const int64_t cnt = hi - lo;
+                    if (cnt <= cap) {
+                        twin[b].push_back(make_int2((int)lo, (int)cnt));
+                        win_cap[b] = std::max(win_cap[b], (int)cnt);
+                    } else {
+                        twin[b].push_back(make_int2(0, 0));
+                    }
+                }
+        }
         // plan the allocation
         arena.want(&d_state[0], 2 * (size_t)N + 2);
         arena.want(&d_state[1], 2 * (size_t)N + 2);
@@ -293,7 +380,12 @@ struct Engine {
         for (int b = 0; b < 3; ++b) {
             n_tiles[b] = (int)tiles[b].size();
             arena.want(&d_tiles[b], tiles[b].size() + 1);
+            arena.want(&d_twin[b], twin[b].size() + 1);
         }
+        arena.want(&d_sell, sell.size());
+        if (perk) arena.want(&d_sellk, sellk.size());
+        arena.want(&d_slice_off, soff.size());
+        arena.want(&d_vinfo, vinfo.size());
         arena.want(&d_views, (size_t)G);
         arena.want(&d_err, 4);
         arena.want(&d_check, 4);
@@ -320,8 +412,14 @@ struct Engine {
         CU(cudaMemcpy(d_rowp, h_rowp.data(), h_rowp.size() * 4, cudaMemcpyHostToDevice));
         if (E > 0) CU(cudaMemcpy(d_ent, ent.data(), E * sizeof(uint2), cudaMemcpyHostToDevice));
         if (perk && E > 0) CU(cudaMemcpy(d_k, kk.data(), E * sizeof(float), cudaMemcpyHostToDevice));
-        for (int b = 0; b < 3; ++b)
+        for (int b = 0; b < 3; ++b) {
             CU(cudaMemcpy(d_tiles[b], tiles[b].data(), tiles[b].size() * sizeof(int4), cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(d_twin[b], twin[b].data(), twin[b].size() * sizeof(int2), cudaMemcpyHostToDevice));
+        }
+        CU(cudaMemcpy(d_sell, sell.data(), sell.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        if (perk) CU(cudaMemcpy(d_sellk, sellk.data(), sellk.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_slice_off, soff.data(), soff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_vinfo, vinfo.data(), vinfo.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
         std::vector<BvhView> views(G);
         for (int g = 0; g < G; ++g)
             views[g] = gin[g].nt > 0 ? bvh[g].view() : BvhView{nullptr, nullptr, nullptr};
@@ -346,7 +444,14 @@ struct Engine {
         return sync();
     }
 
-    int variant() const {
+    int variant(int blk) const {
+        int v = variant();
+        const int bi = block_index(blk);
+        if (stage && bi >= 0 && win_cap[bi] > 0) v |= SV_STAGED;
+        return v;
+    }
+
+    int variant() const {  // without the launch-shape dependent bits
         int v = 0;
         if (perk) v |= SV_PERK;
         if (p.verlet_damping == 1.0f) v |= SV_REFV;
@@ -372,6 +477,7 @@ struct Engine {
         for (int l = 0; l < VISG_MAX_LISTS; ++l) sp.list_k[l] = p.list_k[l];
         sp.n_lists = p.n_lists;
         sp.max_disp = p.max_displacement;
+        sp.margin = p.collision_margin ? 1 : 0;
         return sp;
     }
 
@@ -391,11 +497,17 @@ struct Engine {
         a.check = d_check;
         a.cand = d_cand;
         a.cand_count = d_cand_count;
+        a.sell = d_sell;
+        a.sellk = d_sellk;
+        a.slice_off = d_slice_off;
+        a.vinfo = d_vinfo;
+        a.twin = d_twin[bi];
+        a.win_cap = win_cap[bi];
         a.p = step_params();
         return a;
     }
 
-    cudaError_t launch_one(cudaStream_t s, int from) { return launch_step(args(from, block), variant(), block, grid, s); }
+    cudaError_t launch_one(cudaStream_t s, int from) { return launch_step(args(from, block), variant(block), block, grid, s); }
 
     int capture_chunk(int c) {
         cudaGraph_t g = nullptr;
@@ -459,7 +571,7 @@ struct Engine {
             CU(cudaMemsetAsync(d_err, 0, 4, stream));
             CU(cudaMemsetAsync(d_check, 0, 8, stream));
             CU(cudaStreamSynchronize(stream));
-            if (err & ERR_TIMEOUT) return fail(VISG_ERR_TIMEOUT, "a bounded device wait gave up (LBVH look-back)");
+            if (err & ERR_TIMEOUT) return fail(VISG_ERR_TIMEOUT, "a bounded device wait gave up (LBVH look-back or step stage copy)");
             if (err & ERR_STACK) return fail(VISG_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
             char buf[160];
             std::snprintf(buf, sizeof buf, "diverged: %u non-finite vertices, max step displacement %g (limit %g)", bad,
@@ -502,6 +614,7 @@ struct Engine {
             return fail(VISG_ERR_INVALID_ARG, "body normals must be given iff they were given at creation");
         CU(cudaMemcpyAsync(bvh[g].xyz_in, xyz, (size_t)bvh[g].nv * 12, kind, stream));
         if (nrm) CU(cudaMemcpyAsync(bvh[g].nrm_in, nrm, (size_t)bvh[g].nv * 12, kind, stream));
+        CU(launch_clear_margin(d_state[cur], voff[g], voff[g + 1], stream));  // the body moves
         return body_build(g);
     }
 
@@ -565,8 +678,50 @@ struct Engine {
             if (idx[k] >= (uint32_t)N) return fail(VISG_ERR_INVALID_ARG, "pinned index out of range");
         for (int64_t i = 0; i < N; ++i) h_rowp[i] &= ROW_MASK;
         for (int k = 0; k < n; ++k) h_rowp[idx[k]] |= PIN_BIT;
+        for (int64_t i = 0; i < N; ++i) h_vinfo[i] = (h_vinfo[i] & ROW_MASK) | (h_rowp[i] & PIN_BIT);
         CU(cudaMemcpyAsync(d_rowp, h_rowp.data(), (size_t)N * 4, cudaMemcpyHostToDevice, stream));
+        CU(cudaMemcpyAsync(d_vinfo, h_vinfo.data(), (size_t)N * 4, cudaMemcpyHostToDevice, stream));
         CU(cudaStreamSynchronize(stream));
+        return VISG_OK;
+    }
+
+    // Enqueue, behind the steps issued so far, the read of all positions into host
+    // memory `out`; returns at once.  The unpack runs on the step stream, the copy on
+    // the read-back stream, so the steps issued next overlap the transfer.
+    int read_positions_async(float* out) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
+        if (rb.pending == 2) return fail(VISG_ERR_STATE, "two reads are in flight: wait for one first");
+        if (!rb.copy) {
+            CU(cudaStreamCreateWithFlags(&rb.copy, cudaStreamNonBlocking));
+            CU(cudaHostAlloc((void**)&rb.h_err, 16, cudaHostAllocDefault));
+            for (int k = 0; k < 2; ++k) {
+                CU(cudaMalloc((void**)&rb.d_pos[k], (size_t)N * 12 + 16));
+                CU(cudaEventCreateWithFlags(&rb.unpacked[k], cudaEventDisableTiming));
+                CU(cudaEventCreateWithFlags(&rb.copied[k], cudaEventDisableTiming));
+            }
+        }
+        const int k = rb.next;
+        if (rb.used[k]) CU(cudaStreamWaitEvent(stream, rb.copied[k], 0));  // slot's last copy has left
+        CU(launch_unpack_positions(d_state[cur], N, rb.d_pos[k], stream));
+        CU(cudaMemcpyAsync(rb.h_err + k, d_err, 4, cudaMemcpyDeviceToHost, stream));
+        CU(cudaEventRecord(rb.unpacked[k], stream));
+        CU(cudaStreamWaitEvent(rb.copy, rb.unpacked[k], 0));
+        CU(cudaMemcpyAsync(out, rb.d_pos[k], (size_t)N * 12, cudaMemcpyDeviceToHost, rb.copy));
+        CU(cudaEventRecord(rb.copied[k], rb.copy));
+        rb.used[k] = true;
+        rb.next ^= 1;
+        ++rb.pending;
+        return VISG_OK;
+    }
+
+    // wait for the oldest read in flight; reports device-side errors like a sync
+    int wait_positions() {
+        if (rb.pending == 0) return fail(VISG_ERR_STATE, "no read in flight");
+        const int k = rb.pending == 2 ? rb.next : rb.next ^ 1;
+        --rb.pending;
+        CU(cudaEventSynchronize(rb.copied[k]));
+        if (rb.h_err[k] != 0u) return sync();  // a device-side error: report it (and clear it)
         return VISG_OK;
     }
 
@@ -750,6 +905,21 @@ struct Engine {
         return sync();
     }
 
+    int set_launch(int blk, int ctas) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        const int bi = block_index(blk);
+        if (bi < 0) return fail(VISG_ERR_INVALID_ARG, "block must be 128, 256 or 512");
+        if (ctas < 0 || (ctas > 0 && ctas > step_max_ctas_per_sm(variant(blk), blk, win_cap[bi])))
+            return fail(VISG_ERR_INVALID_ARG, "ctas_per_sm out of range for this block size");
+        if (int r = sync()) return r;
+        if (blk != block || ctas * sm_count != grid) {
+            block = blk;
+            grid = ctas * sm_count;
+            destroy_graphs();
+        }
+        return VISG_OK;
+    }
+
     // time every launch shape on this engine's data; keep the fastest; restore the state
     int autotune(int* out_block, int* out_ctas) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
@@ -767,18 +937,32 @@ struct Engine {
             e = cudaMemcpyAsync(bs + 2 * N, d_state[cur ^ 1], 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice,
                                 stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(bn, d_normal, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        // every candidate starts from the same state, so all are timed on the same contacts
+        auto restore = [&]() {
+            cur = cur0;
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_state[cur], bs, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                    stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_state[cur ^ 1], bs + 2 * N, 2 * (size_t)N * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_normal, bn, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        };
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         float best = 1e30f;
-        int best_block = block, best_grid = grid, best_ctas = 0, best_split = split;
-        const int split0 = split;
+        int best_block = block, best_grid = grid, best_ctas = 0, best_split = split, best_stage = stage;
+        const int split0 = split, stage0 = stage;
         const int n_split = (p.collide && any_body) ? 2 : 1;
-        for (int sv = 0; sv < n_split * 3 && e == cudaSuccess; ++sv) {
-            split = sv / 3;
+        for (int sv = 0; sv < 2 * n_split * 3 && e == cudaSuccess; ++sv) {
+            stage = sv / (3 * n_split);
+            split = (sv / 3) % n_split;
             const int bi = sv % 3;
             const int blk = kBlocks[bi];
-            const int occ = step_max_ctas_per_sm(variant(), blk);
+            if (stage && win_cap[bi] == 0) continue;
+            const int occ = step_max_ctas_per_sm(variant(blk), blk, win_cap[bi]);
             std::vector<int> ctas;
             for (int c = 1; c <= occ; c *= 2) ctas.push_back(c);
             if (occ > 0 && ctas.back() != occ) ctas.push_back(occ);
@@ -787,13 +971,14 @@ struct Engine {
                 const int gr = c == 0 ? 0 : c * sm_count;
                 auto run = [&](int k) {
                     for (int s = 0; s < k && e == cudaSuccess; ++s) {
-                        e = launch_step(args(cur, blk), variant(), blk, gr, stream);
+                        e = launch_step(args(cur, blk), variant(blk), blk, gr, stream);
                         cur ^= 1;
                     }
                 };
+                restore();
                 run(1);
                 cudaEventRecord(e0, stream);
-                run(4);
+                run(6);
                 cudaEventRecord(e1, stream);
                 if (e == cudaSuccess) e = cudaEventSynchronize(e1);
                 float ms = 0;
@@ -804,27 +989,24 @@ struct Engine {
                     best_grid = gr;
                     best_ctas = c;
                     best_split = split;
+                    best_stage = stage;
                 }
             }
         }
         split = split0;
-        cur = cur0;
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_state[cur], bs, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_state[cur ^ 1], bs + 2 * N, 2 * (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice,
-                                stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_normal, bn, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+        stage = stage0;
+        restore();
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         cudaFree(bs);
         cudaFree(bn);
         if (e != cudaSuccess) return cuda_fail(e, "autotune");
-        if (best_block != block || best_grid != grid || best_split != split) {
+        if (best_block != block || best_grid != grid || best_split != split || best_stage != stage) {
             block = best_block;
             grid = best_grid;
             split = best_split;
+            stage = best_stage;
             destroy_graphs();
         }
         if (out_block) *out_block = block;
@@ -874,6 +1056,8 @@ void visg_default_params(VisgParams* p) {
     p->max_displacement = 1.0f;
     p->use_graph = 1;
     p->split_collision = 1;
+    p->stage_neighbours = 1;
+    p->collision_margin = 1;
 }
 
 const char* visg_version(void) { return "visg-gb300 1.0 (sm_103a)"; }
@@ -954,6 +1138,16 @@ int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n) {
 int visg_get_positions(VisgSim* sim, float* out, int32_t on_device) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.get_positions(0, out, on_device);
+}
+
+int visg_read_positions_async(VisgSim* sim, float* out) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.read_positions_async(out);
+}
+
+int visg_wait_positions(VisgSim* sim) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.wait_positions();
 }
 
 int visg_get_state(VisgSim* sim, float* x, float* xo, float* n) {
@@ -1067,6 +1261,16 @@ int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t 
     return b->eng.get_positions(garment, out, on_device);
 }
 
+int visg_batch_read_positions_async(VisgBatch* b, float* out) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.read_positions_async(out);
+}
+
+int visg_batch_wait_positions(VisgBatch* b) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.wait_positions();
+}
+
 int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.set_vertex(garment, idx, xyz);
@@ -1085,6 +1289,11 @@ int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* xyz, cons
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.autotune(block, ctas);
+}
+
+int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.set_launch(block, ctas);
 }
 
 int visg_batch_info(VisgBatch* b, int32_t* ng, int64_t* nv, int64_t* ne, int64_t* nt) {

@@ -4,13 +4,22 @@
 //   cloth state, double-buffered: 2 float4 per vertex
 //        [x.x x.y x.z v.x] [v.y v.z flags 0]             32 B, one sector per gather
 //        v = (x - x_old) / dt, computed once per step by the vertex's own thread;
-//        x_old is x (flag XO_IS_X) or the x of the same vertex in the other buffer
+//        x_old is x (flag XO_IS_X) or the x of the same vertex in the other buffer;
+//        the last word is the collision margin: a proven lower bound of the distance
+//        from x to every leaf box of the garment's body (0 = unknown)
 //   contact normal (previous step):  float4 per vertex, read only when flags says so
 //   rowp:   u32 per vertex + 1, merged CSR row offsets; bit 31 = vertex pinned
 //   ent:    uint2 per directed spring {end | list << 30, rest}         8 B
 //   kent:   f32 per directed spring, only with per-spring stiffness
-//   tiles:  int4 per tile {garment, first vertex, end vertex, 0}; a tile never
-//           straddles two garments
+//   sell:   the same springs in sliced-ELL order for the step kernel: a slice is 32
+//           consecutive vertices of one garment, padded to its longest row; entry k of
+//           lane l of slice s sits at slice_off[s] + 32 k + l, so the k-th springs of a
+//           warp are one contiguous 256-byte run (sellk: stiffness, same layout)
+//   vinfo:  u32 per vertex: merged row length, bit 31 = pinned
+//   tiles:  int4 per tile {garment, first vertex, end vertex, first slice}; a tile
+//           never straddles two garments.  twin: int2 per tile {lo, count}, the
+//           window of vertex records its springs touch (itself included) that a
+//           TMA bulk copy stages in shared memory; count 0 = read from global memory
 //   per body: LBVH nodes (64 B: both children's boxes and links), leaves (32 B:
 //           v0 and the face normal), root record; build scratch (sort buffers,
 //           look-back status words, handshake flags)
@@ -113,6 +122,7 @@ struct StepParams {
     float list_k[VISG_MAX_LISTS];
     int n_lists;
     float max_disp;
+    int margin;  // keep each vertex's proven distance to its body's leaf boxes (collision margin)
 };
 
 struct StepArgs {
@@ -129,6 +139,12 @@ struct StepArgs {
     uint32_t* check;  // [0] max |dx| bits, [1] non-finite count
     int2* cand;       // split collision: {vertex, garment} of the vertices inside their body's box
     uint32_t* cand_count;
+    const uint2* sell;        // sliced-ELL springs (see the layout above)
+    const float* sellk;       // per-entry stiffness in the same layout, with SV_PERK
+    const uint32_t* slice_off;
+    const uint32_t* vinfo;
+    const int2* twin;         // per tile neighbour window, with SV_STAGED
+    int win_cap;              // records per shared-memory stage buffer
     StepParams p;
 };
 
@@ -139,9 +155,12 @@ enum StepVariant : int {
     SV_CHECK = 8,     // divergence check
     SV_KD0 = 16,      // spring damping exactly +0
     SV_SPLIT = 32,    // collision in its own kernel over a compacted candidate list
+    SV_STAGED = 64,   // neighbour windows staged in shared memory by TMA bulk copies
 };
+// dynamic shared memory of a launch: two stage buffers of win_cap records + barriers
+int step_smem_bytes(int variant, int win_cap);
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
-int step_max_ctas_per_sm(int variant, int block);
+int step_max_ctas_per_sm(int variant, int block, int win_cap);
 
 // first-hit queries of external points against one body
 cudaError_t launch_query(BvhView v, const float* pts, int n, int* leaf, int* inside, float* dist,
@@ -154,6 +173,9 @@ cudaError_t launch_unpack_state(const float4* state, const float4* other, const 
 // x/xo/nrm may be NULL (kept); dt recomputes v = (x - x_old) / dt
 cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x,
                               const float* xo, const float* nrm, float dt, cudaStream_t s);
+
+// forget the collision margin of vertices [v0, v1) (their body moved)
+cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s);
 
 // number of vertices with the contact flag set, accumulated into *count
 cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long long* count, cudaStream_t s);

@@ -4,8 +4,10 @@
 // GB300: one thread per vertex, persistent CTAs walking a tile table (a tile is
 // BLOCK consecutive vertices of one garment, so one launch covers any number of
 // garments of uneven size), 32-byte interleaved state records read with two
-// float4 loads for the vertex and for every CSR neighbour, one merged CSR of
-// 8-byte entries with the list id in the top bits (no atomics), the previous
+// float4 loads for the vertex and for every spring neighbour (from a window of
+// records that a TMA bulk copy staged in shared memory while the previous tile was
+// computed), springs of all lists merged into one sliced-ELL table of 8-byte
+// entries with the list id in the top bits (no atomics), the previous
 // contact normal read only for vertices that had a contact, and the collision
 // (collision_response_projection, verlet.cu:24-50) fused behind a warp vote on the
 // body's root box.  Arithmetic follows the reference operation by operation with
@@ -20,6 +22,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+
 #include "visg_internal.cuh"
 
 namespace visg {
@@ -33,16 +38,39 @@ __device__ __forceinline__ bool in_box(f3 p, float4 lo, float4 hi) {  // BBox::i
     return (p.x >= lo.x && p.x <= hi.x) && (p.y >= lo.y && p.y <= hi.y) && (p.z >= lo.z && p.z <= hi.z);
 }
 
+// Lower bound of the L-infinity distance from p to the closed box [lo, hi]: the
+// largest per-axis gap, each rounded down (0 or less when p is inside).
+__device__ __forceinline__ float box_gap(f3 p, float4 lo, float4 hi) {
+    const float gx = fmaxf(__fsub_rd(lo.x, p.x), __fsub_rd(p.x, hi.x));
+    const float gy = fmaxf(__fsub_rd(lo.y, p.y), __fsub_rd(p.y, hi.y));
+    const float gz = fmaxf(__fsub_rd(lo.z, p.z), __fsub_rd(p.z, hi.z));
+    return fmaxf(gx, fmaxf(gy, gz));
+}
+
+// Upper bound of max_axis |a - b| (each difference rounded up).
+__device__ __forceinline__ float disp_bound(f3 a, f3 b) {
+    const float dx = __fsub_ru(fmaxf(a.x, b.x), fminf(a.x, b.x));
+    const float dy = __fsub_ru(fmaxf(a.y, b.y), fminf(a.y, b.y));
+    const float dz = __fsub_ru(fmaxf(a.z, b.z), fminf(a.z, b.z));
+    return fmaxf(dx, fmaxf(dy, dz));
+}
+
 // D_BVH::intersect semantics: children tested pairwise; an overlapping leaf child is
 // returned before any descent (A before B); both internal -> descend A, push B.
 // A depth-first walk visits every internal node at most once, so `budget` (the
 // number of internal nodes) bounds the loop even on a corrupted tree.
-__device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int node, int budget, f3 p, int* err) {
+// With GAP, a query that finds no leaf also returns in `gap` a lower bound of the
+// distance from p to every leaf box: every leaf lies under a child box the walk
+// rejected, and a node's box contains its children's boxes.
+template <bool GAP>
+__device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int node, int budget, f3 p, int* err,
+                                         float& gap) {
     int stack[kStack];
     int sp = 0;
     while (true) {
         if (--budget < 0) {
             atomicOr(err, ERR_STACK);
+            gap = 0.0f;
             return -1;
         }
         const Node* nd = nodes + node;
@@ -52,6 +80,10 @@ __device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int nod
         const bool ol = in_box(p, alo, ahi), orr = in_box(p, blo, bhi);
         if (ol && la < 0) return ~la;
         if (orr && lb < 0) return ~lb;
+        if (GAP) {
+            if (!ol) gap = fminf(gap, box_gap(p, alo, ahi));
+            if (!orr) gap = fminf(gap, box_gap(p, blo, bhi));
+        }
         const bool tl = ol && la >= 0, tr = orr && lb >= 0;
         if (!tl && !tr) {
             if (sp == 0) return -1;
@@ -61,6 +93,7 @@ __device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int nod
             if (tl && tr) {
                 if (sp == kStack) {
                     atomicOr(err, ERR_STACK);
+                    gap = 0.0f;
                     return -1;
                 }
                 stack[sp++] = lb;
@@ -73,7 +106,8 @@ __device__ __forceinline__ int query_leaf(const BvhView& bv, int n_leaves, int r
                                           f3 p, int* err) {
     if (n_leaves <= 0 || !in_box(p, top_lo, top_hi)) return -1;
     if (n_leaves == 1) return 0;
-    return first_hit(bv.nodes, root, n_leaves, p, err);
+    float gap = 0.0f;
+    return first_hit<false>(bv.nodes, root, n_leaves, p, err, gap);
 }
 
 // Force of one CSR spring on the vertex at x moving with velocity vel (verlet.cu:64-84).
@@ -103,29 +137,45 @@ __device__ __forceinline__ float pick(int f, float k0, float k1, float k2, float
     return f == 0 ? k0 : (f == 1 ? k1 : (f == 2 ? k2 : k3));
 }
 
+// Where a tile's vertex records come from: global memory through the read-only
+// path, or the tile's window [lo, lo + count) staged in shared memory.
+struct GlobalRecords {
+    const float4* __restrict__ p;
+    __device__ __forceinline__ float4 r0(int j) const { return __ldg(p + 2 * j); }
+    __device__ __forceinline__ float4 r1(int j) const { return __ldg(p + 2 * j + 1); }
+};
+struct SharedRecords {
+    const float4* p;
+    int lo;
+    __device__ __forceinline__ float4 r0(int j) const { return p[2 * (j - lo)]; }
+    __device__ __forceinline__ float4 r1(int j) const { return p[2 * (j - lo) + 1]; }
+};
+
 struct SpringIn {
     uint2 en;
     float4 t0, t1;
     float k;
 };
 
-__device__ __forceinline__ SpringIn load_spring(const StepArgs& a, const float4* __restrict__ sin, uint32_t e,
-                                                bool perk) {
+// entry e of a sliced-ELL row: ep/kp point at the row's entry 0, entries 32 apart
+template <class Rec>
+__device__ __forceinline__ SpringIn load_spring(const Rec& rec, const uint2* __restrict__ ep,
+                                                const float* __restrict__ kp, int e, bool perk) {
     SpringIn s;
-    s.en = __ldg(&a.ent[e]);
+    s.en = __ldg(ep + 32 * e);
     const int j = (int)(s.en.x & END_MASK);
-    s.t0 = __ldg(&sin[2 * j]);
-    s.t1 = __ldg(&sin[2 * j + 1]);
-    s.k = perk ? __ldg(&a.kent[e]) : 0.0f;
+    s.t0 = rec.r0(j);
+    s.t1 = rec.r1(j);
+    s.k = perk ? __ldg(kp + 32 * e) : 0.0f;
     return s;
 }
 
-// Sum of the spring forces of row [rp, re) into F, list by list as the reference
+// Sum of the n spring forces of one row into F, list by list as the reference
 // does (force += list sum, verlet.cu:148-149), entries in CSR order.  Springs are
 // evaluated two at a time (independent chains) and accumulated in order.
-template <bool KD0>
-__device__ __forceinline__ f3 spring_sum(const StepArgs& a, const float4* __restrict__ sin, uint32_t rp,
-                                         uint32_t re, f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
+template <bool KD0, class Rec>
+__device__ __forceinline__ f3 spring_sum(const Rec& rec, const uint2* __restrict__ ep, const float* __restrict__ kp,
+                                         int n, f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
     const float k0 = P.list_k[0], k1 = P.list_k[1], k2 = P.list_k[2], k3 = P.list_k[3];
     f3 acc = mk3(0.0f, 0.0f, 0.0f);
     int list = 0;
@@ -138,10 +188,10 @@ __device__ __forceinline__ f3 spring_sum(const StepArgs& a, const float4* __rest
         }
         acc = add(acc, sf);
     };
-    uint32_t e = rp;
-    for (; e + 1 < re; e += 2) {
-        const SpringIn sa = load_spring(a, sin, e, perk);
-        const SpringIn sb = load_spring(a, sin, e + 1, perk);
+    int e = 0;
+    for (; e + 1 < n; e += 2) {
+        const SpringIn sa = load_spring(rec, ep, kp, e, perk);
+        const SpringIn sb = load_spring(rec, ep, kp, e + 1, perk);
         const float ka = perk ? sa.k : pick((int)(sa.en.x >> LIST_SHIFT), k0, k1, k2, k3);
         const float kb = perk ? sb.k : pick((int)(sb.en.x >> LIST_SHIFT), k0, k1, k2, k3);
         const f3 fa = spring_force<KD0>(x, vel, sa.t0, sa.t1, ka, __uint_as_float(sa.en.y), P.kd, eps3);
@@ -149,8 +199,8 @@ __device__ __forceinline__ f3 spring_sum(const StepArgs& a, const float4* __rest
         take(sa, fa);
         take(sb, fb);
     }
-    if (e < re) {
-        const SpringIn sa = load_spring(a, sin, e, perk);
+    if (e < n) {
+        const SpringIn sa = load_spring(rec, ep, kp, e, perk);
         const float ka = perk ? sa.k : pick((int)(sa.en.x >> LIST_SHIFT), k0, k1, k2, k3);
         take(sa, spring_force<KD0>(x, vel, sa.t0, sa.t1, ka, __uint_as_float(sa.en.y), P.kd, eps3));
     }
@@ -162,102 +212,227 @@ __device__ __forceinline__ f3 spring_sum(const StepArgs& a, const float4* __rest
     return F;
 }
 
+// One thread's vertex of tile td = {garment, first vertex, end vertex, first slice}.
 // State record of vertex i in buffer b: [x.xyz, v.x] [v.y, v.z, flags, 0] with
 // v = (x - x_old) / dt.  x_old is x itself when FLAG_XO_IS_X is set (after a
 // contact, a pin or update_vertex) and otherwise the previous step's x, which is
 // still in the other buffer: the step reads it there before overwriting it.
-template <int BLOCK, bool COLL, bool KD0, bool SPLIT>
-__global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
+template <bool COLL, bool KD0, bool SPLIT, class Rec>
+__device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, const int4 td, const int refv,
+                                            const int check, const int perk, float& my_disp, uint32_t& my_bad) {
     const StepParams& P = a.p;
     const f3 grav = mk3(P.gx, P.gy, P.gz);
     const f3 eps3 = mk3(kFltEpsilon, kFltEpsilon, kFltEpsilon);
-    const float4* __restrict__ sin = a.state_in;
-    float my_disp = 0.0f;
-    uint32_t my_bad = 0;
-    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
-        const int4 td = __ldg(&a.tiles[tile]);
-        const int i = td.y + (int)threadIdx.x;
-        const bool active = i < td.z;
-        const int ii = active ? i : td.y;
-        const float4 s0 = __ldg(&sin[2 * ii]);
-        const float4 s1 = __ldg(&sin[2 * ii + 1]);
-        const f3 x = mk3(s0.x, s0.y, s0.z);
-        const f3 vel = mk3(s0.w, s1.x, s1.y);
-        const uint32_t flags = __float_as_uint(s1.z);
-        uint32_t rp = __ldg(&a.rowp[ii]);
-        const uint32_t re = __ldg(&a.rowp[ii + 1]) & ROW_MASK;
-        const bool pinned = (rp & PIN_BIT) != 0u;
-        rp &= ROW_MASK;
-        f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
-        bool has_n = false;
-        if (!pinned) {
-            const f3 xo = (flags & FLAG_XO_IS_X) ? x : xyz(a.state_out[2 * ii]);
-            f3 np = mk3(0.0f, 0.0f, 0.0f);
-            if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
-            f3 F = add(mul(grav, P.mass), mul(vel, P.damp));
-            F = spring_sum<KD0>(a, sin, rp, re, x, vel, F, P, perk != 0, eps3);
-            F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
-            const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
-            if (refv) xn = add(sub(add(x, x), xo), adt);
-            else xn = add(add(x, mul(P.gamma, sub(x, xo))), adt);
-            xon = x;
+    const int i = td.y + (int)threadIdx.x;
+    const bool active = i < td.z;
+    const int ii = active ? i : td.y;
+    const float4 s0 = rec.r0(ii);
+    const float4 s1 = rec.r1(ii);
+    const f3 x = mk3(s0.x, s0.y, s0.z);
+    const f3 vel = mk3(s0.w, s1.x, s1.y);
+    const uint32_t flags = __float_as_uint(s1.z);
+    const uint32_t vi = __ldg(&a.vinfo[ii]);
+    const bool pinned = (vi & PIN_BIT) != 0u;
+    f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
+    bool has_n = false;
+    if (active && !pinned) {
+        const int lane = (int)(threadIdx.x & 31u);
+        const uint32_t sb = __ldg(&a.slice_off[td.w + (int)(threadIdx.x >> 5)]) + (uint32_t)lane;
+        const f3 xo = (flags & FLAG_XO_IS_X) ? x : xyz(a.state_out[2 * ii]);
+        f3 np = mk3(0.0f, 0.0f, 0.0f);
+        if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
+        f3 F = add(mul(grav, P.mass), mul(vel, P.damp));
+        F = spring_sum<KD0>(rec, a.sell + sb, perk ? a.sellk + sb : nullptr, (int)(vi & ROW_MASK), x, vel, F, P,
+                            perk != 0, eps3);
+        F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
+        const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
+        if (refv) xn = add(sub(add(x, x), xo), adt);
+        else xn = add(add(x, mul(P.gamma, sub(x, xo))), adt);
+        xon = x;
+    }
+    // Collision margin: s1.w holds a lower bound of the distance from x to every leaf
+    // box of the body, proven by the last query that found no leaf.  While the vertex
+    // has moved less than that since, the query would find no leaf again and is
+    // skipped; the bound shrinks by each step's displacement (rounded up).
+    float skin = 0.0f;
+    bool far = false;
+    if (COLL && P.margin && active && !pinned) {
+        skin = __fsub_rd(s1.w, disp_bound(xn, x));
+        far = skin > 0.0f;
+    }
+    if (COLL && SPLIT) {
+        // split collision: queue the vertices inside their body's box (one atomic per
+        // warp); k_collide traverses them with fully populated warps
+        const BvhView bv = a.bodies[td.x];
+        bool cand = false;
+        if (bv.root != nullptr)
+            cand = active && !pinned && bv.root->n_leaves > 0 && in_box(xn, bv.root->top_lo, bv.root->top_hi);
+        if (!cand) skin = 0.0f;
+        cand = cand && !far;
+        if (cand) skin = 0.0f;  // k_collide stores the new bound
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        if (m) {
+            const int lane = (int)(threadIdx.x & 31u), leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.cand_count, (uint32_t)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (cand) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, td.x);
         }
-        if (COLL && SPLIT) {
-            // split collision: queue the vertices inside their body's box (one atomic per
-            // warp); k_collide traverses them with fully populated warps
-            const BvhView bv = a.bodies[td.x];
-            bool cand = false;
-            if (bv.root != nullptr)
-                cand = active && !pinned && bv.root->n_leaves > 0 && in_box(xn, bv.root->top_lo, bv.root->top_hi);
-            const unsigned m = __ballot_sync(0xffffffffu, cand);
-            if (m) {
-                const int lane = (int)(threadIdx.x & 31u), leader = __ffs(m) - 1;
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(a.cand_count, (uint32_t)__popc(m));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (cand) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, td.x);
-            }
-        } else if (COLL) {
-            const BvhView bv = a.bodies[td.x];
-            if (bv.root != nullptr) {
-                const int nl = bv.root->n_leaves;
-                const int rt = bv.root->root;
-                const float4 tlo = bv.root->top_lo, thi = bv.root->top_hi;
-                const bool cand = active && !pinned && nl > 0 && in_box(xn, tlo, thi);
-                if (__any_sync(0xffffffffu, cand)) {
-                    if (cand) {
-                        const int leaf = nl == 1 ? 0 : first_hit(bv.nodes, rt, nl, xn, a.err);
-                        if (leaf >= 0) {
-                            const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
-                            const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
-                            const f3 n = mk3(L0.w, L1.x, L1.y);
-                            const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), n);
-                            if (!(d > 0.0f)) {
-                                xn = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), n));
-                                xon = xn;
-                                nn = n;
-                                has_n = true;
-                            }
+    } else if (COLL) {
+        const BvhView bv = a.bodies[td.x];
+        if (bv.root != nullptr) {
+            const int nl = bv.root->n_leaves;
+            const int rt = bv.root->root;
+            const float4 tlo = bv.root->top_lo, thi = bv.root->top_hi;
+            bool cand = active && !pinned && nl > 0 && in_box(xn, tlo, thi);
+            if (!cand) skin = 0.0f;
+            cand = cand && !far;
+            if (__any_sync(0xffffffffu, cand)) {
+                if (cand) {
+                    float gap = __int_as_float(0x7f800000);  // +inf
+                    const int leaf = nl == 1 ? 0 : first_hit<true>(bv.nodes, rt, nl, xn, a.err, gap);
+                    skin = (leaf < 0 && P.margin) ? gap : 0.0f;
+                    if (leaf >= 0) {
+                        const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
+                        const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
+                        const f3 n = mk3(L0.w, L1.x, L1.y);
+                        const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), n);
+                        if (!(d > 0.0f)) {
+                            xn = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), n));
+                            xon = xn;
+                            nn = n;
+                            has_n = true;
                         }
                     }
                 }
             }
         }
-        if (active) {
-            const bool xo_is_x = pinned || has_n;
-            const f3 vn = divs(sub(xn, xon), P.dt);
-            const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u);
-            a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, vn.x);
-            a.state_out[2 * i + 1] = make_float4(vn.y, vn.z, __uint_as_float(fl), 0.0f);
-            if (has_n) a.normal[i] = make_float4(nn.x, nn.y, nn.z, 0.0f);
-            if (check) {
-                const float dd = fmaxf(fabsf(__fsub_rn(xn.x, x.x)),
-                                       fmaxf(fabsf(__fsub_rn(xn.y, x.y)), fabsf(__fsub_rn(xn.z, x.z))));
-                if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(vn.x) || !isfinite(vn.y) ||
-                    !isfinite(vn.z))
-                    ++my_bad;
-                else
-                    my_disp = fmaxf(my_disp, dd);
+    }
+    if (active) {
+        const bool xo_is_x = pinned || has_n;
+        const f3 vn = divs(sub(xn, xon), P.dt);
+        const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u);
+        a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, vn.x);
+        a.state_out[2 * i + 1] = make_float4(vn.y, vn.z, __uint_as_float(fl), skin > 0.0f ? skin : 0.0f);
+        if (has_n) a.normal[i] = make_float4(nn.x, nn.y, nn.z, 0.0f);
+        if (check) {
+            const float dd = fmaxf(fabsf(__fsub_rn(xn.x, x.x)),
+                                   fmaxf(fabsf(__fsub_rn(xn.y, x.y)), fabsf(__fsub_rn(xn.z, x.z))));
+            if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(vn.x) || !isfinite(vn.y) ||
+                !isfinite(vn.z))
+                ++my_bad;
+            else
+                my_disp = fmaxf(my_disp, dd);
+        }
+    }
+}
+
+// ---- TMA bulk copies into shared memory, completed on an mbarrier ----------------------
+constexpr int kBarBytes = 128;                 // two 8-byte mbarriers, padded
+constexpr uint64_t kWaitNs = 1000000000ull;    // a stage that has not landed after 1 s is an error
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+// one arrival that also announces `bytes` of transactions, then the copy that completes them
+__device__ __forceinline__ void bulk_stage(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// bounded wait for the phase of the given parity to complete
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_test(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_test(bar, parity))
+        if (global_ns() - t0 > kWaitNs) return false;
+    return true;
+}
+
+// thread 0: stage the window of `tile` (if it has one) into buffer `b`
+__device__ __forceinline__ void stage_window(const StepArgs& a, int tile, uint32_t win, uint32_t bar) {
+    const int2 tw = __ldg(&a.twin[tile]);
+    if (tw.y > 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the buffer come first
+        bulk_stage(win, a.state_in + 2 * (size_t)tw.x, (uint32_t)tw.y * 32u, bar);
+    }
+}
+
+// The fused step: persistent CTAs walk the tile table.  With STAGED, thread 0 copies
+// the next tile's window of vertex records (a contiguous run of 32-byte records,
+// usually the tile and a band of rows either side) into the other shared-memory
+// buffer with one TMA bulk copy while the CTA computes the current tile, so the
+// spring gathers hit shared memory; tiles whose window exceeds the buffer read
+// global memory.  Waits are bounded: a copy that has not landed after kWaitNs sets
+// ERR_TIMEOUT, and the CTA waits (again bounded) for its copies in flight and exits.
+template <int BLOCK, bool COLL, bool KD0, bool SPLIT, bool STAGED>
+__global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    float my_disp = 0.0f;
+    uint32_t my_bad = 0;
+    const GlobalRecords grec{a.state_in};
+    if (!STAGED) {
+        for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x)
+            vertex_step<COLL, KD0, SPLIT>(a, grec, __ldg(&a.tiles[tile]), refv, check, perk, my_disp, my_bad);
+    } else {
+        const uint32_t bar = smem_addr(dyn_smem);
+        const uint32_t win = bar + kBarBytes;
+        const float4* swin = reinterpret_cast<const float4*>(dyn_smem + kBarBytes);
+        const uint32_t wbytes = (uint32_t)a.win_cap * 32u;
+        if (threadIdx.x == 0) {
+            mbar_init(bar);
+            mbar_init(bar + 8);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && (int)blockIdx.x < a.n_tiles) stage_window(a, blockIdx.x, win, bar);
+        uint32_t par = 0;  // parity of the next phase of each buffer's barrier
+        int b = 0;
+        for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, b ^= 1) {
+            const int nxt = tile + (int)gridDim.x;
+            if (threadIdx.x == 0 && nxt < a.n_tiles) stage_window(a, nxt, win + (uint32_t)(b ^ 1) * wbytes, bar + 8u * (b ^ 1));
+            const int4 td = __ldg(&a.tiles[tile]);
+            const int2 tw = __ldg(&a.twin[tile]);
+            bool ok = true;
+            if (tw.y > 0) {
+                ok = __all_sync(0xffffffffu, mbar_wait(bar + 8u * b, (par >> b) & 1u));
+                par ^= 1u << b;
+                if (ok)
+                    vertex_step<COLL, KD0, SPLIT>(a, SharedRecords{swin + 2 * b * a.win_cap, tw.x}, td, refv, check,
+                                                  perk, my_disp, my_bad);
+            } else {
+                vertex_step<COLL, KD0, SPLIT>(a, grec, td, refv, check, perk, my_disp, my_bad);
+            }
+            if (__syncthreads_or(!ok)) {
+                // a copy did not land: record it, let this CTA's copies in flight finish, leave
+                if (threadIdx.x == 0) {
+                    atomicOr(a.err, ERR_TIMEOUT);
+                    if (tw.y > 0) mbar_wait(bar + 8u * b, ((par >> b) & 1u) ^ 1u);
+                    if (nxt < a.n_tiles && __ldg(&a.twin[nxt]).y > 0) mbar_wait(bar + 8u * (b ^ 1), (par >> (b ^ 1)) & 1u);
+                }
+                return;
             }
         }
     }
@@ -288,8 +463,12 @@ __global__ void __launch_bounds__(COLLIDE_BLOCK) k_collide(const StepArgs a) {
         const int nl = bv.root->n_leaves;
         const float4 s0 = a.state_out[2 * c.x];
         f3 xn = mk3(s0.x, s0.y, s0.z);
-        const int leaf = nl == 1 ? 0 : first_hit(bv.nodes, bv.root->root, nl, xn, a.err);
-        if (leaf < 0) continue;
+        float gap = __int_as_float(0x7f800000);  // +inf
+        const int leaf = nl == 1 ? 0 : first_hit<true>(bv.nodes, bv.root->root, nl, xn, a.err, gap);
+        if (leaf < 0) {
+            if (a.p.margin) reinterpret_cast<float*>(a.state_out + 2 * c.x + 1)[3] = gap;  // the record's w
+            continue;
+        }
         const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
         const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
         const f3 nrm = mk3(L0.w, L1.x, L1.y);
@@ -306,13 +485,46 @@ __global__ void __launch_bounds__(COLLIDE_BLOCK) k_collide(const StepArgs a) {
 
 int g_collide_grid = 0;
 
-template <int BLOCK, bool KD0>
-cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int check, int perk, int grid,
+// the step kernel instance of a variant
+template <int BLOCK, bool KD0, bool STAGED>
+using StepKernel = void (*)(const StepArgs, const int, const int, const int);
+
+template <int BLOCK, bool KD0, bool STAGED>
+StepKernel<BLOCK, KD0, STAGED> step_kernel(bool coll, bool split) {
+    if (coll && split) return k_step<BLOCK, true, KD0, true, STAGED>;
+    if (coll) return k_step<BLOCK, true, KD0, false, STAGED>;
+    return k_step<BLOCK, false, KD0, false, STAGED>;
+}
+
+// largest dynamic shared memory each kernel instance has been opened up to (per device)
+std::mutex g_smem_mu;
+std::map<std::pair<int, const void*>, int> g_smem_set;
+
+cudaError_t allow_smem(const void* fn, int bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    int& cur = g_smem_set[{dev, fn}];
+    if (cur >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
+template <int BLOCK, bool KD0, bool STAGED>
+cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int check, int perk, int grid, int smem,
                       cudaStream_t s) {
+    const auto fn = step_kernel<BLOCK, KD0, STAGED>(coll, split);
+    cudaError_t e = allow_smem((const void*)fn, smem);
+    if (e != cudaSuccess) return e;
     if (coll && split) {
-        cudaError_t e = cudaMemsetAsync(a.cand_count, 0, sizeof(uint32_t), s);
+        e = cudaMemsetAsync(a.cand_count, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
-        k_step<BLOCK, true, KD0, true><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
+    }
+    fn<<<grid, BLOCK, smem, s>>>(a, refv, check, perk);
+    if (coll && split) {
         if (g_collide_grid == 0) {
             int dev = 0, sms = 0, occ = 0;
             cudaGetDevice(&dev);
@@ -321,10 +533,6 @@ cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int ch
             g_collide_grid = sms * (occ > 0 ? occ : 1);
         }
         k_collide<<<g_collide_grid, COLLIDE_BLOCK, 0, s>>>(a);
-    } else if (coll) {
-        k_step<BLOCK, true, KD0, false><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
-    } else {
-        k_step<BLOCK, false, KD0, false><<<grid, BLOCK, 0, s>>>(a, refv, check, perk);
     }
     return cudaGetLastError();
 }
@@ -335,23 +543,33 @@ cudaError_t launch_block(const StepArgs& a, int variant, int grid, cudaStream_t 
     const int check = (variant & SV_CHECK) ? 1 : 0;
     const int perk = (variant & SV_PERK) ? 1 : 0;
     const bool coll = (variant & SV_COLLIDE) != 0, split = (variant & SV_SPLIT) != 0;
-    if (variant & SV_KD0) return launch_kd<BLOCK, true>(a, coll, split, refv, check, perk, grid, s);
-    return launch_kd<BLOCK, false>(a, coll, split, refv, check, perk, grid, s);
+    const int smem = step_smem_bytes(variant, a.win_cap);
+    if (variant & SV_STAGED) {
+        if (variant & SV_KD0) return launch_kd<BLOCK, true, true>(a, coll, split, refv, check, perk, grid, smem, s);
+        return launch_kd<BLOCK, false, true>(a, coll, split, refv, check, perk, grid, smem, s);
+    }
+    if (variant & SV_KD0) return launch_kd<BLOCK, true, false>(a, coll, split, refv, check, perk, grid, 0, s);
+    return launch_kd<BLOCK, false, false>(a, coll, split, refv, check, perk, grid, 0, s);
 }
 
-template <int BLOCK, bool KD0>
-int occupancy_kd(bool coll, bool split) {
+template <int BLOCK, bool KD0, bool STAGED>
+int occupancy_kd(bool coll, bool split, int smem) {
+    const auto fn = step_kernel<BLOCK, KD0, STAGED>(coll, split);
+    if (allow_smem((const void*)fn, smem) != cudaSuccess) return 0;
     int n = 0;
-    if (coll && split) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, KD0, true>, BLOCK, 0);
-    else if (coll) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, true, KD0, false>, BLOCK, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step<BLOCK, false, KD0, false>, BLOCK, 0);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, BLOCK, smem) != cudaSuccess) return 0;
     return n;
 }
 
 template <int BLOCK>
-int occupancy_block(int variant) {
+int occupancy_block(int variant, int win_cap) {
     const bool coll = (variant & SV_COLLIDE) != 0, split = (variant & SV_SPLIT) != 0;
-    return (variant & SV_KD0) ? occupancy_kd<BLOCK, true>(coll, split) : occupancy_kd<BLOCK, false>(coll, split);
+    const int smem = step_smem_bytes(variant, win_cap);
+    if (variant & SV_STAGED)
+        return (variant & SV_KD0) ? occupancy_kd<BLOCK, true, true>(coll, split, smem)
+                                  : occupancy_kd<BLOCK, false, true>(coll, split, smem);
+    return (variant & SV_KD0) ? occupancy_kd<BLOCK, true, false>(coll, split, 0)
+                              : occupancy_kd<BLOCK, false, false>(coll, split, 0);
 }
 
 __global__ void k_query(BvhView bv, const float* __restrict__ pts, int n, int* leaf, int* inside, float* dist,
@@ -431,6 +649,11 @@ __global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, c
     st[2 * i + 1] = make_float4(v.y, v.z, __uint_as_float(fl), 0.0f);
 }
 
+__global__ void k_clear_margin(float4* st, int64_t v0, int64_t v1) {
+    const int64_t i = v0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < v1) reinterpret_cast<float*>(st + 2 * i + 1)[3] = 0.0f;
+}
+
 __global__ void k_count_contacts(const float4* __restrict__ st, int64_t n, unsigned long long* count) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool c = i < n && (__float_as_uint(st[2 * i + 1].z) & FLAG_HAS_NORMAL);
@@ -467,11 +690,15 @@ cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cud
     }
 }
 
-int step_max_ctas_per_sm(int variant, int block) {
+int step_smem_bytes(int variant, int win_cap) {
+    return (variant & SV_STAGED) ? kBarBytes + 2 * 32 * win_cap : 0;
+}
+
+int step_max_ctas_per_sm(int variant, int block, int win_cap) {
     switch (block) {
-        case 128: return occupancy_block<128>(variant);
-        case 256: return occupancy_block<256>(variant);
-        case 512: return occupancy_block<512>(variant);
+        case 128: return occupancy_block<128>(variant, win_cap);
+        case 256: return occupancy_block<256>(variant, win_cap);
+        case 512: return occupancy_block<512>(variant, win_cap);
         default: return 0;
     }
 }
@@ -493,6 +720,12 @@ cudaError_t launch_unpack_state(const float4* state, const float4* other, const 
                                 float* xo, float* nrm, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     k_unpack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s) {
+    if (v1 <= v0) return cudaSuccess;
+    k_clear_margin<<<grid_for(v1 - v0, 256), 256, 0, s>>>(state, v0, v1);
     return cudaGetLastError();
 }
 

@@ -29,6 +29,8 @@ class VisgParams(C.Structure):
         ("max_displacement", C.c_float),
         ("use_graph", C.c_int32),
         ("split_collision", C.c_int32),
+        ("stage_neighbours", C.c_int32),
+        ("collision_margin", C.c_int32),
     ]
 
 
@@ -52,13 +54,16 @@ def reference_params(n_lists: int = 2) -> VisgParams:
     p.max_displacement = 1.0
     p.use_graph = 1
     p.split_collision = 1
+    p.stage_neighbours = 1
+    p.collision_margin = 1
     return p
 
 
 def make_params(n_lists: int, dt: float, mass: float, gravity=(0.0, -9.8, 0.0), force_damping=0.0,
                 spring_damping=0.0, verlet_damping=1.0, thickness=0.003, box_depth=0.01,
                 list_k=(100.0, 2.0, 2.0, 2.0), collide=1, check_every=0, max_displacement=1.0,
-                use_graph=1, split_collision=1) -> VisgParams:
+                use_graph=1, split_collision=1, stage_neighbours=1,
+                collision_margin=1) -> VisgParams:
     p = VisgParams()
     p.dt, p.mass = dt, mass
     p.gravity[:] = tuple(gravity)
@@ -69,4 +74,6 @@ def make_params(n_lists: int, dt: float, mass: float, gravity=(0.0, -9.8, 0.0), 
     p.list_k[:] = tuple(k[:VISG_MAX_LISTS])
     p.collide, p.check_every, p.max_displacement, p.use_graph = collide, check_every, max_displacement, use_graph
     p.split_collision = split_collision
+    p.stage_neighbours = stage_neighbours
+    p.collision_margin = collision_margin
     return p

@@ -222,6 +222,78 @@ def test_split_and_fused_collision_identical(lists):
     assert a.count_contacts() > 10
 
 
+@pytest.mark.parametrize("split", [0, 1])
+def test_staged_and_global_neighbours_identical(split):
+    cloth, cl, body, p = ref_scene(side=40, subdiv=3)
+    p.split_collision = split
+    pg = reference_params(len(cl))
+    for f, _ in vs.VisgParams._fields_:
+        setattr(pg, f, getattr(p, f))
+    pg.stage_neighbours = 0
+    a = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    b = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=pg)
+    a.simulate(150)
+    b.simulate(150)
+    for u, v in zip(a.state(), b.state()):
+        assert np.array_equal(u, v)
+    assert a.count_contacts() > 10
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_collision_margin_on_and_off_identical(split):
+    # the sheet falls onto the sphere and slides: vertices approach the body, touch,
+    # leave; with the margin the first-hit query is skipped while it provably misses
+    cloth = scenes.grid_cloth(48, 1.0, 0.0)
+    body = scenes.icosphere(4, 0.3, (0.05, -0.34, 0.0))
+    p = config_params(substeps=2)
+    p.split_collision = split
+    q = config_params(substeps=2)
+    for f, _ in vs.VisgParams._fields_:
+        setattr(q, f, getattr(p, f))
+    q.collision_margin = 0
+    a = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=p, pinned=cloth.pinned)
+    b = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=q, pinned=cloth.pinned)
+    for _ in range(6):
+        a.simulate(60)
+        b.simulate(60)
+        for u, v in zip(a.state(), b.state()):
+            assert np.array_equal(u, v)
+    assert a.count_contacts() > 10
+
+
+def permuted(cloth, lists, order):
+    """The same cloth with its vertices renumbered: new vertex k is old vertex order[k]."""
+    inv = np.empty_like(order)
+    inv[order] = np.arange(len(order))
+    xyz = np.ascontiguousarray(cloth.xyz[order])
+    out = []
+    for sl in lists:
+        src = np.repeat(np.arange(len(sl.row) - 1), np.diff(sl.row.astype(np.int64)))
+        out.append(scenes._csr_from_pairs(len(order), inv[src], inv[sl.ent["end"].astype(np.int64)], xyz))
+    return xyz, out
+
+
+def test_scrambled_vertex_order_vs_oracle():
+    # the second half of the vertices in random order: those tiles' neighbour windows
+    # exceed the shared-memory stage and read global memory, the first half's are staged
+    cloth, cl, body, p = ref_scene(side=64, subdiv=3)
+    n = len(cloth.xyz)
+    order = np.arange(n)
+    order[n // 2:] = np.random.default_rng(3).permutation(order[n // 2:])
+    xyz, lists = permuted(cloth, cl, order)
+    win = []
+    for t in range(0, n, 256):
+        js = [t, min(t + 256, n) - 1]
+        for sl in lists:
+            js += list(sl.ent["end"][sl.row[t]:sl.row[min(t + 256, n)]])
+        win.append(max(js) - min(js) + 1)
+    assert min(win) <= 1536 < max(win)
+    sc = scenes.Cloth(xyz=xyz, lists=lists)
+    g, o = run_pair(sc, lists, body, p, 120)
+    x, nrm = assert_state_equal(g, o)
+    assert (np.abs(nrm).sum(1) > 0).sum() > 10
+
+
 def test_set_vertex_and_state_roundtrip():
     cloth, cl, body, p = ref_scene(side=16, subdiv=2)
     g = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
@@ -269,6 +341,49 @@ def test_batch_equals_plain_per_garment():
         x = s.positions()
         assert np.array_equal(b.positions(gi), x)
         assert np.array_equal(allx[b.offsets[gi]:b.offsets[gi + 1]], x)
+
+
+def test_pipelined_position_reads_equal_synchronous_reads():
+    cloth, cl, body, p = ref_scene(side=24, subdiv=2)
+    a = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    s = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    with pytest.raises(RuntimeError):
+        a.wait_positions()  # nothing in flight
+    got = [np.full((a.n, 3), np.nan, np.float32) for _ in range(8)]
+    want = []
+    for k in range(8):
+        a.simulate(1)
+        a.read_positions_async(got[k])
+        if k > 0:
+            a.wait_positions()
+        s.simulate(1)
+        want.append(s.positions())
+    extra = np.empty((a.n, 3), np.float32)
+    a.simulate(1)
+    a.read_positions_async(extra)  # the second read in flight
+    with pytest.raises(RuntimeError):
+        a.read_positions_async(np.empty((a.n, 3), np.float32))  # a third is refused
+    a.wait_positions()
+    a.wait_positions()
+    s.simulate(1)
+    assert np.array_equal(extra, s.positions())
+    for k in range(8):
+        assert np.array_equal(got[k], want[k]), k
+
+
+def test_batch_pipelined_reads():
+    cloth, cl, body, p = ref_scene(side=20, subdiv=2)
+    b = vs.BatchSimulator(p)
+    for _ in range(3):
+        b.add(cloth.xyz, cl, body.xyz, body.tris, body.normals)
+    b.finalize()
+    n = int(b.offsets[-1])
+    got = [np.empty((n, 3), np.float32) for _ in range(2)]
+    for k in range(5):
+        b.step(1)
+        b.read_positions_async(got[k % 2])
+        b.wait_positions()
+        assert np.array_equal(got[k % 2], b.positions())
 
 
 def test_batch_autotune_keeps_state_and_results():
