@@ -120,8 +120,9 @@ struct Engine {
     uint2* d_sell = nullptr;                         // sliced-ELL springs
     float* d_sellk = nullptr;
     uint32_t* d_slice_off = nullptr;
-    uint32_t* d_vinfo = nullptr;
-    std::vector<uint32_t> h_vinfo;                   // row length | pin bit, per vertex
+    uint2* d_vcount = nullptr;                      // springs per list | pin bit, per vertex
+    std::vector<uint2> h_vcount;
+    uint32_t* d_wild = nullptr;                      // sticky: a record was not tame
     int stage = 1;                                   // stage neighbour windows (autotuned)
     BvhView* d_views = nullptr;
     std::vector<BvhBuffers> bvh;
@@ -313,8 +314,7 @@ struct Engine {
         for (int g = 0; g < G; ++g) slice0[g + 1] = slice0[g] + (gin[g].N + 31) / 32;
         const int64_t S = slice0[G];
         std::vector<uint32_t> soff(S + 1, 0);
-        std::vector<uint32_t>& vinfo = h_vinfo;
-        vinfo.assign(N, 0u);
+        h_vcount.assign(N, make_uint2(0u, 0u));
         auto row_len = [&](int64_t v) { return (h_rowp[v + 1] & ROW_MASK) - (h_rowp[v] & ROW_MASK); };
         {
             uint64_t c2 = 0;
@@ -338,7 +338,11 @@ struct Engine {
                 const int64_t s = slice0[g] + (v - voff[g]) / 32;
                 const int64_t lane = (v - voff[g]) % 32;
                 const uint32_t rp = h_rowp[v] & ROW_MASK, n = row_len(v);
-                vinfo[v] = n | (h_rowp[v] & PIN_BIT);
+                uint32_t c[VISG_MAX_LISTS] = {0u, 0u, 0u, 0u};
+                for (uint32_t k = 0; k < n; ++k) ++c[ent[rp + k].x >> LIST_SHIFT];
+                if (c[0] > 0xffffu || c[1] > 0xffffu || c[2] > 0xffffu || c[3] > 0x7fffu)
+                    return fail(VISG_ERR_UNSUPPORTED, "more than 65535 springs of one list at one vertex");
+                h_vcount[v] = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16) | (h_rowp[v] & PIN_BIT));
                 for (uint32_t k = 0; k < n; ++k) {
                     sell[soff[s] + 32 * (int64_t)k + lane] = ent[rp + k];
                     if (perk) sellk[soff[s] + 32 * (int64_t)k + lane] = kk[rp + k];
@@ -385,7 +389,8 @@ struct Engine {
         arena.want(&d_sell, sell.size());
         if (perk) arena.want(&d_sellk, sellk.size());
         arena.want(&d_slice_off, soff.size());
-        arena.want(&d_vinfo, vinfo.size());
+        arena.want(&d_vcount, h_vcount.size());
+        arena.want(&d_wild, 4);
         arena.want(&d_views, (size_t)G);
         arena.want(&d_err, 4);
         arena.want(&d_check, 4);
@@ -419,7 +424,9 @@ struct Engine {
         CU(cudaMemcpy(d_sell, sell.data(), sell.size() * sizeof(uint2), cudaMemcpyHostToDevice));
         if (perk) CU(cudaMemcpy(d_sellk, sellk.data(), sellk.size() * sizeof(float), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(d_slice_off, soff.data(), soff.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(d_vinfo, vinfo.data(), vinfo.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_vcount, h_vcount.data(), h_vcount.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        CU(cudaMemsetAsync(d_wild, 0, 4, stream));
+        CU(launch_check_tame(d_state[0], N, d_wild, stream));
         std::vector<BvhView> views(G);
         for (int g = 0; g < G; ++g)
             views[g] = gin[g].nt > 0 ? bvh[g].view() : BvhView{nullptr, nullptr, nullptr};
@@ -500,7 +507,8 @@ struct Engine {
         a.sell = d_sell;
         a.sellk = d_sellk;
         a.slice_off = d_slice_off;
-        a.vinfo = d_vinfo;
+        a.vcount = d_vcount;
+        a.wild = d_wild;
         a.twin = d_twin[bi];
         a.win_cap = win_cap[bi];
         a.p = step_params();
@@ -667,7 +675,7 @@ struct Engine {
         CU(cudaMemcpyAsync(d_sv_idx, h_sv, (size_t)n * 4, cudaMemcpyHostToDevice, stream));
         CU(cudaMemcpyAsync(d_sv_xyz, h_sv + (size_t)sv_cap * 4, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
         CU(cudaEventRecord(sv_done, stream));
-        CU(launch_set_vertices(d_state[cur], d_sv_idx, d_sv_xyz, n, p.dt, stream));
+        CU(launch_set_vertices(d_state[cur], d_sv_idx, d_sv_xyz, n, p.dt, d_wild, stream));
         return VISG_OK;
     }
 
@@ -678,9 +686,9 @@ struct Engine {
             if (idx[k] >= (uint32_t)N) return fail(VISG_ERR_INVALID_ARG, "pinned index out of range");
         for (int64_t i = 0; i < N; ++i) h_rowp[i] &= ROW_MASK;
         for (int k = 0; k < n; ++k) h_rowp[idx[k]] |= PIN_BIT;
-        for (int64_t i = 0; i < N; ++i) h_vinfo[i] = (h_vinfo[i] & ROW_MASK) | (h_rowp[i] & PIN_BIT);
+        for (int64_t i = 0; i < N; ++i) h_vcount[i].y = (h_vcount[i].y & ROW_MASK) | (h_rowp[i] & PIN_BIT);
         CU(cudaMemcpyAsync(d_rowp, h_rowp.data(), (size_t)N * 4, cudaMemcpyHostToDevice, stream));
-        CU(cudaMemcpyAsync(d_vinfo, h_vinfo.data(), (size_t)N * 4, cudaMemcpyHostToDevice, stream));
+        CU(cudaMemcpyAsync(d_vcount, h_vcount.data(), (size_t)N * sizeof(uint2), cudaMemcpyHostToDevice, stream));
         CU(cudaStreamSynchronize(stream));
         return VISG_OK;
     }
@@ -777,8 +785,7 @@ struct Engine {
         if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
         if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
         CU(launch_pack_state(d_state[cur], d_state[cur ^ 1], d_normal, N, x ? sx : nullptr, xo ? sxo : nullptr,
-                             nrm ? sn : nullptr, p.dt,
-                             stream));
+                             nrm ? sn : nullptr, p.dt, d_wild, stream));
         CU(cudaStreamSynchronize(stream));
         return VISG_OK;
     }

@@ -15,7 +15,8 @@
 //           consecutive vertices of one garment, padded to its longest row; entry k of
 //           lane l of slice s sits at slice_off[s] + 32 k + l, so the k-th springs of a
 //           warp are one contiguous 256-byte run (sellk: stiffness, same layout)
-//   vinfo:  u32 per vertex: merged row length, bit 31 = pinned
+//   vcount: uint2 per vertex: the row's springs per list (16 bits each, list 3 15
+//           bits), bit 31 of .y = pinned
 //   tiles:  int4 per tile {garment, first vertex, end vertex, first slice}; a tile
 //           never straddles two garments.  twin: int2 per tile {lo, count}, the
 //           window of vertex records its springs touch (itself included) that a
@@ -142,7 +143,8 @@ struct StepArgs {
     const uint2* sell;        // sliced-ELL springs (see the layout above)
     const float* sellk;       // per-entry stiffness in the same layout, with SV_PERK
     const uint32_t* slice_off;
-    const uint32_t* vinfo;
+    const uint2* vcount;      // per vertex: springs per list, 16 bits each (list 3: 15), bit 63 = pinned
+    uint32_t* wild;           // sticky: some record had |x| or |v| >= 1e15 (or NaN)
     const int2* twin;         // per tile neighbour window, with SV_STAGED
     int win_cap;              // records per shared-memory stage buffer
     StepParams p;
@@ -172,7 +174,7 @@ cudaError_t launch_unpack_state(const float4* state, const float4* other, const 
                                 float* xo, float* nrm, cudaStream_t s);
 // x/xo/nrm may be NULL (kept); dt recomputes v = (x - x_old) / dt
 cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x,
-                              const float* xo, const float* nrm, float dt, cudaStream_t s);
+                              const float* xo, const float* nrm, float dt, uint32_t* wild, cudaStream_t s);
 
 // forget the collision margin of vertices [v0, v1) (their body moved)
 cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s);
@@ -181,8 +183,11 @@ cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStrea
 cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long long* count, cudaStream_t s);
 
 // scatter (idx[k] -> x = x_old = xyz[k]) into the state, keeping the contact flag
-cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt,
+cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt, uint32_t* wild,
                                 cudaStream_t s);
+
+// set *wild when some record of [0, n) has a component of |x| or |v| >= 1e15 (or NaN)
+cudaError_t launch_check_tame(const float4* state, int64_t n, uint32_t* wild, cudaStream_t s);
 
 // ---- adjoint ----------------------------------------------------------------------------
 // Packed float3 arrays of one recorded step: x, x_old and the contact normal entering

@@ -110,31 +110,22 @@ __device__ __forceinline__ int query_leaf(const BvhView& bv, int n_leaves, int r
     return first_hit<false>(bv.nodes, root, n_leaves, p, err, gap);
 }
 
-// Force of one CSR spring on the vertex at x moving with velocity vel (verlet.cu:64-84).
+// Force of one spring on the vertex at x moving with velocity vel (verlet.cu:64-84):
+//   c = -k (|d| - L0) + kd (dv.d) / |d|,  force = c * normalize(d),  d = x - x_j + FLT_EPSILON
 // t0/t1 is the neighbour's record: position and velocity (p2 - p2_old) / dt, stored
-// once per step by the neighbour's own thread with the same IEEE division.
-// With KD0 (spring damping exactly +0) the damping term is +0 * RN(dot / dist), a
-// signed zero: left + (+-0) == left for every finite non-zero left, so the damping
-// term is evaluated only when left is zero or not finite.
-template <bool KD0>
-__device__ __forceinline__ f3 spring_force(f3 x, f3 vel, float4 t0, float4 t1, float ks, float rest, float kd,
+// once per step by the neighbour's own thread with the same IEEE division; nk = -k.
+// FAST drops the damping term, for spring damping exactly +0: see row_forces.
+template <bool FAST>
+__device__ __forceinline__ f3 spring_force(f3 x, f3 vel, float4 t0, float4 t1, float nk, float rest, float kd,
                                            f3 eps3) {
-    const f3 p2 = mk3(t0.x, t0.y, t0.z);
-    const f3 dP = add(sub(x, p2), eps3);
+    const f3 dP = add(sub(x, mk3(t0.x, t0.y, t0.z)), eps3);
     const float dist = __fsqrt_rn(dot(dP, dP));
-    const float left = __fmul_rn(-ks, __fsub_rn(dist, rest));
-    float c;
-    if (KD0 && left != 0.0f && isfinite(left)) {
-        c = left;
-    } else {
+    float c = __fmul_rn(nk, __fsub_rn(dist, rest));
+    if (!FAST) {
         const f3 dV = sub(vel, mk3(t0.w, t1.x, t1.y));
-        c = __fadd_rn(left, __fmul_rn(kd, __fdiv_rn(dot(dV, dP), dist)));
+        c = __fadd_rn(c, __fmul_rn(kd, __fdiv_rn(dot(dV, dP), dist)));
     }
     return mul(c, mul(dP, __frcp_rn(dist)));  // normalize(dP) = dP * (1 / |dP|)
-}
-
-__device__ __forceinline__ float pick(int f, float k0, float k1, float k2, float k3) {
-    return f == 0 ? k0 : (f == 1 ? k1 : (f == 2 ? k2 : k3));
 }
 
 // Where a tile's vertex records come from: global memory through the read-only
@@ -151,65 +142,58 @@ struct SharedRecords {
     __device__ __forceinline__ float4 r1(int j) const { return p[2 * (j - lo) + 1]; }
 };
 
-struct SpringIn {
-    uint2 en;
-    float4 t0, t1;
-    float k;
-};
-
-// entry e of a sliced-ELL row: ep/kp point at the row's entry 0, entries 32 apart
-template <class Rec>
-__device__ __forceinline__ SpringIn load_spring(const Rec& rec, const uint2* __restrict__ ep,
-                                                const float* __restrict__ kp, int e, bool perk) {
-    SpringIn s;
-    s.en = __ldg(ep + 32 * e);
-    const int j = (int)(s.en.x & END_MASK);
-    s.t0 = rec.r0(j);
-    s.t1 = rec.r1(j);
-    s.k = perk ? __ldg(kp + 32 * e) : 0.0f;
-    return s;
+// Sum of springs [e, end) of one list of a sliced-ELL row (ep/kp at the row's entry
+// 0, entries 32 apart), in CSR order, two at a time (independent chains).
+template <bool FAST, class Rec>
+__device__ __forceinline__ f3 list_sum(const Rec& rec, const uint2* __restrict__ ep, const float* __restrict__ kp,
+                                       int e, const int end, const float nk, const bool perk, f3 x, f3 vel,
+                                       float kd, f3 eps3) {
+    f3 acc = mk3(0.0f, 0.0f, 0.0f);
+    for (; e + 1 < end; e += 2) {
+        const uint2 ea = __ldg(ep + 32 * e), eb = __ldg(ep + 32 * (e + 1));
+        const int ja = (int)(ea.x & END_MASK), jb = (int)(eb.x & END_MASK);
+        const float4 a0 = rec.r0(ja), b0 = rec.r0(jb);
+        const float4 a1 = FAST ? a0 : rec.r1(ja), b1 = FAST ? b0 : rec.r1(jb);
+        const float ka = perk ? -__ldg(kp + 32 * e) : nk;
+        const float kb = perk ? -__ldg(kp + 32 * (e + 1)) : nk;
+        const f3 fa = spring_force<FAST>(x, vel, a0, a1, ka, __uint_as_float(ea.y), kd, eps3);
+        const f3 fb = spring_force<FAST>(x, vel, b0, b1, kb, __uint_as_float(eb.y), kd, eps3);
+        acc = add(add(acc, fa), fb);
+    }
+    if (e < end) {
+        const uint2 ea = __ldg(ep + 32 * e);
+        const int ja = (int)(ea.x & END_MASK);
+        const float4 a0 = rec.r0(ja);
+        const float4 a1 = FAST ? a0 : rec.r1(ja);
+        const float ka = perk ? -__ldg(kp + 32 * e) : nk;
+        acc = add(acc, spring_force<FAST>(x, vel, a0, a1, ka, __uint_as_float(ea.y), kd, eps3));
+    }
+    return acc;
 }
 
-// Sum of the n spring forces of one row into F, list by list as the reference
-// does (force += list sum, verlet.cu:148-149), entries in CSR order.  Springs are
-// evaluated two at a time (independent chains) and accumulated in order.
-template <bool KD0, class Rec>
-__device__ __forceinline__ f3 spring_sum(const Rec& rec, const uint2* __restrict__ ep, const float* __restrict__ kp,
-                                         int n, f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
-    const float k0 = P.list_k[0], k1 = P.list_k[1], k2 = P.list_k[2], k3 = P.list_k[3];
-    f3 acc = mk3(0.0f, 0.0f, 0.0f);
-    int list = 0;
-    auto take = [&](const SpringIn& s, f3 sf) {
-        const int f = (int)(s.en.x >> LIST_SHIFT);
-        while (list < f) {
-            F = add(F, acc);
-            acc = mk3(0.0f, 0.0f, 0.0f);
-            ++list;
-        }
-        acc = add(acc, sf);
-    };
+// F + the spring forces of one vertex, list by list as the reference does
+// (force += list sum, verlet.cu:148-149); cnt holds the row's per-list counts.
+template <bool FAST, class Rec>
+__device__ __forceinline__ f3 row_forces(const Rec& rec, const uint2* __restrict__ ep, const float* __restrict__ kp,
+                                         uint2 cnt, f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
     int e = 0;
-    for (; e + 1 < n; e += 2) {
-        const SpringIn sa = load_spring(rec, ep, kp, e, perk);
-        const SpringIn sb = load_spring(rec, ep, kp, e + 1, perk);
-        const float ka = perk ? sa.k : pick((int)(sa.en.x >> LIST_SHIFT), k0, k1, k2, k3);
-        const float kb = perk ? sb.k : pick((int)(sb.en.x >> LIST_SHIFT), k0, k1, k2, k3);
-        const f3 fa = spring_force<KD0>(x, vel, sa.t0, sa.t1, ka, __uint_as_float(sa.en.y), P.kd, eps3);
-        const f3 fb = spring_force<KD0>(x, vel, sb.t0, sb.t1, kb, __uint_as_float(sb.en.y), P.kd, eps3);
-        take(sa, fa);
-        take(sb, fb);
-    }
-    if (e < n) {
-        const SpringIn sa = load_spring(rec, ep, kp, e, perk);
-        const float ka = perk ? sa.k : pick((int)(sa.en.x >> LIST_SHIFT), k0, k1, k2, k3);
-        take(sa, spring_force<KD0>(x, vel, sa.t0, sa.t1, ka, __uint_as_float(sa.en.y), P.kd, eps3));
-    }
-    while (list < P.n_lists) {
-        F = add(F, acc);
-        acc = mk3(0.0f, 0.0f, 0.0f);
-        ++list;
+#pragma unroll
+    for (int l = 0; l < VISG_MAX_LISTS; ++l) {
+        if (l < P.n_lists) {
+            const int n = (int)(((l < 2 ? cnt.x : cnt.y) >> (16 * (l & 1))) & (l == 3 ? 0x7fffu : 0xffffu));
+            F = add(F, list_sum<FAST>(rec, ep, kp, e, e + n, -P.list_k[l], perk, x, vel, P.kd, eps3));
+            e += n;
+        }
     }
     return F;
+}
+
+// |x| < 1e15 and |v| < 1e15 in every component (false for NaN): while every record
+// satisfies this, RN(dv.d / |d|) is finite for every spring (|dv.d| < 3 (2e15)^2,
+// |d| within a factor ~2 of max |d_i| unless it underflows to 0).
+__device__ __forceinline__ bool tame(f3 x, f3 v) {
+    const float m = 1e15f;
+    return fabsf(x.x) < m && fabsf(x.y) < m && fabsf(x.z) < m && fabsf(v.x) < m && fabsf(v.y) < m && fabsf(v.z) < m;
 }
 
 // One thread's vertex of tile td = {garment, first vertex, end vertex, first slice}.
@@ -219,7 +203,8 @@ __device__ __forceinline__ f3 spring_sum(const Rec& rec, const uint2* __restrict
 // still in the other buffer: the step reads it there before overwriting it.
 template <bool COLL, bool KD0, bool SPLIT, class Rec>
 __device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, const int4 td, const int refv,
-                                            const int check, const int perk, float& my_disp, uint32_t& my_bad) {
+                                            const int check, const int perk, const bool wild, float& my_disp,
+                                            uint32_t& my_bad) {
     const StepParams& P = a.p;
     const f3 grav = mk3(P.gx, P.gy, P.gz);
     const f3 eps3 = mk3(kFltEpsilon, kFltEpsilon, kFltEpsilon);
@@ -231,8 +216,8 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, c
     const f3 x = mk3(s0.x, s0.y, s0.z);
     const f3 vel = mk3(s0.w, s1.x, s1.y);
     const uint32_t flags = __float_as_uint(s1.z);
-    const uint32_t vi = __ldg(&a.vinfo[ii]);
-    const bool pinned = (vi & PIN_BIT) != 0u;
+    const uint2 cnt = __ldg(&a.vcount[ii]);
+    const bool pinned = (cnt.y & PIN_BIT) != 0u;
     f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
     bool has_n = false;
     if (active && !pinned) {
@@ -241,9 +226,23 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, c
         const f3 xo = (flags & FLAG_XO_IS_X) ? x : xyz(a.state_out[2 * ii]);
         f3 np = mk3(0.0f, 0.0f, 0.0f);
         if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
-        f3 F = add(mul(grav, P.mass), mul(vel, P.damp));
-        F = spring_sum<KD0>(rec, a.sell + sb, perk ? a.sellk + sb : nullptr, (int)(vi & ROW_MASK), x, vel, F, P,
-                            perk != 0, eps3);
+        const f3 F0 = add(mul(grav, P.mass), mul(vel, P.damp));
+        const uint2* ep = a.sell + sb;
+        const float* kp = perk ? a.sellk + sb : nullptr;
+        f3 F;
+        if (KD0) {
+            // Spring damping is +0: the reference adds +0 * RN(dv.d / |d|) to every c.
+            // Without it c differs at most in the sign of a zero, which changes no sum
+            // (a zero force adds nothing to sums that start at +0, which never become -0),
+            // as long as RN(dv.d / |d|) is finite (guaranteed while every record is tame;
+            // the wild flag says when one was not) or c is not finite (then F is not
+            // finite either: such rows are recomputed with the damping term).
+            F = row_forces<true>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
+            if (wild || !(isfinite(F.x) && isfinite(F.y) && isfinite(F.z)))
+                F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
+        } else {
+            F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
+        }
         F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
         const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
         if (refv) xn = add(sub(add(x, x), xo), adt);
@@ -308,9 +307,11 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, c
             }
         }
     }
+    bool untamed = false;
     if (active) {
         const bool xo_is_x = pinned || has_n;
         const f3 vn = divs(sub(xn, xon), P.dt);
+        untamed = !tame(xn, vn);
         const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u);
         a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, vn.x);
         a.state_out[2 * i + 1] = make_float4(vn.y, vn.z, __uint_as_float(fl), skin > 0.0f ? skin : 0.0f);
@@ -325,6 +326,7 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, c
                 my_disp = fmaxf(my_disp, dd);
         }
     }
+    if (__any_sync(0xffffffffu, untamed) && (threadIdx.x & 31u) == 0u) atomicOr(a.wild, 1u);
 }
 
 // ---- TMA bulk copies into shared memory, completed on an mbarrier ----------------------
@@ -393,9 +395,10 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
     float my_disp = 0.0f;
     uint32_t my_bad = 0;
     const GlobalRecords grec{a.state_in};
+    const bool wild = *reinterpret_cast<const volatile uint32_t*>(a.wild) != 0u;
     if (!STAGED) {
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x)
-            vertex_step<COLL, KD0, SPLIT>(a, grec, __ldg(&a.tiles[tile]), refv, check, perk, my_disp, my_bad);
+            vertex_step<COLL, KD0, SPLIT>(a, grec, __ldg(&a.tiles[tile]), refv, check, perk, wild, my_disp, my_bad);
     } else {
         const uint32_t bar = smem_addr(dyn_smem);
         const uint32_t win = bar + kBarBytes;
@@ -421,9 +424,9 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
                 par ^= 1u << b;
                 if (ok)
                     vertex_step<COLL, KD0, SPLIT>(a, SharedRecords{swin + 2 * b * a.win_cap, tw.x}, td, refv, check,
-                                                  perk, my_disp, my_bad);
+                                                  perk, wild, my_disp, my_bad);
             } else {
-                vertex_step<COLL, KD0, SPLIT>(a, grec, td, refv, check, perk, my_disp, my_bad);
+                vertex_step<COLL, KD0, SPLIT>(a, grec, td, refv, check, perk, wild, my_disp, my_bad);
             }
             if (__syncthreads_or(!ok)) {
                 // a copy did not land: record it, let this CTA's copies in flight finish, leave
@@ -480,6 +483,7 @@ __global__ void __launch_bounds__(COLLIDE_BLOCK) k_collide(const StepArgs a) {
         a.state_out[2 * c.x + 1] =
             make_float4(vn.y, vn.z, __uint_as_float(FLAG_HAS_NORMAL | FLAG_XO_IS_X), 0.0f);
         a.normal[c.x] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        if (!tame(xn, vn)) atomicOr(a.wild, 1u);
     }
 }
 
@@ -627,7 +631,7 @@ __global__ void k_unpack_state(const float4* __restrict__ st, const float4* __re
 // x == nullptr keeps x, etc.  x_old is written into the other buffer and v is
 // recomputed as (x - x_old) / dt; a vertex has a stored normal iff it is non-zero.
 __global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, const float* x, const float* xo,
-                             const float* nrm, float dt) {
+                             const float* nrm, float dt, uint32_t* wild) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 s0 = st[2 * i], s1 = st[2 * i + 1];
@@ -647,6 +651,14 @@ __global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, c
     other[2 * i] = make_float4(xov.x, xov.y, xov.z, 0.0f);
     st[2 * i] = make_float4(xv.x, xv.y, xv.z, v.x);
     st[2 * i + 1] = make_float4(v.y, v.z, __uint_as_float(fl), 0.0f);
+    if (!tame(xv, v)) atomicOr(wild, 1u);
+}
+
+__global__ void k_check_tame(const float4* __restrict__ st, int64_t n, uint32_t* wild) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 s0 = st[2 * i], s1 = st[2 * i + 1];
+    if (!tame(mk3(s0.x, s0.y, s0.z), mk3(s0.w, s1.x, s1.y))) atomicOr(wild, 1u);
 }
 
 __global__ void k_clear_margin(float4* st, int64_t v0, int64_t v1) {
@@ -664,7 +676,7 @@ __global__ void k_count_contacts(const float4* __restrict__ st, int64_t n, unsig
 // update_vertex (simulation.cu:253-257): x = x_old = p, so v = (p - p) / dt; the
 // stored contact normal is kept
 __global__ void k_set_vertices(float4* st, const uint32_t* __restrict__ idx, const float* __restrict__ xyz3, int n,
-                               float dt) {
+                               float dt, uint32_t* wild) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int64_t v = idx[k];
@@ -673,6 +685,7 @@ __global__ void k_set_vertices(float4* st, const uint32_t* __restrict__ idx, con
     const uint32_t fl = (__float_as_uint(st[2 * v + 1].z) & FLAG_HAS_NORMAL) | FLAG_XO_IS_X;
     st[2 * v] = make_float4(p.x, p.y, p.z, vel.x);
     st[2 * v + 1] = make_float4(vel.y, vel.z, __uint_as_float(fl), 0.0f);
+    if (!tame(p, vel)) atomicOr(wild, 1u);
 }
 
 inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -723,6 +736,12 @@ cudaError_t launch_unpack_state(const float4* state, const float4* other, const 
     return cudaGetLastError();
 }
 
+cudaError_t launch_check_tame(const float4* state, int64_t n, uint32_t* wild, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_check_tame<<<grid_for(n, 256), 256, 0, s>>>(state, n, wild);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s) {
     if (v1 <= v0) return cudaSuccess;
     k_clear_margin<<<grid_for(v1 - v0, 256), 256, 0, s>>>(state, v0, v1);
@@ -735,16 +754,17 @@ cudaError_t launch_count_contacts(const float4* state, int64_t n, unsigned long 
     return cudaGetLastError();
 }
 
-cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt, cudaStream_t s) {
+cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float* xyz, int n, float dt, uint32_t* wild,
+                                cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_set_vertices<<<grid_for(n, 256), 256, 0, s>>>(state, idx, xyz, n, dt);
+    k_set_vertices<<<grid_for(n, 256), 256, 0, s>>>(state, idx, xyz, n, dt, wild);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x, const float* xo,
-                              const float* nrm, float dt, cudaStream_t s) {
+                              const float* nrm, float dt, uint32_t* wild, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm, dt);
+    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm, dt, wild);
     return cudaGetLastError();
 }
 

@@ -415,6 +415,39 @@ def test_divergence_reported():
     assert e.value.code == -5
 
 
+def test_zero_damping_fast_path_exact_far_from_origin():
+    # positions beyond 1e15 m mark the state untamed: every row takes the full formula
+    cloth = scenes.grid_cloth(16, 1.0, 0.0)
+    xyz = cloth.xyz.copy()
+    xyz[:, 0] += np.float32(2e15)
+    p = config_params(substeps=2)  # spring damping exactly +0
+    g = vs.Simulator(xyz, cloth.lists, params=p, pinned=cloth.pinned)
+    o = OracleSim(p, xyz, cloth.lists, prec=4, pinned=cloth.pinned)
+    g.simulate(12)
+    o.step(12)
+    assert_state_equal(g, o)
+
+
+def test_zero_damping_fast_path_exact_through_blow_up():
+    # an unstable step size: the state grows through huge and non-finite values; the
+    # fast path must agree with the oracle bit for bit all the way (NaNs compared as NaN)
+    cloth = scenes.grid_cloth(12, 1.0, 0.0)
+    p = config_params(substeps=1)
+    g = vs.Simulator(cloth.xyz, cloth.lists, params=p, pinned=cloth.pinned)
+    o = OracleSim(p, cloth.xyz, cloth.lists, prec=4, pinned=cloth.pinned)
+    seen_huge = seen_nan = False
+    for _ in range(40):
+        g.simulate(5)
+        o.step(5)
+        x, xo, n = g.state()
+        ox, oxo, on = (a.astype(np.float32) for a in o.state())
+        assert np.array_equal(x, ox, equal_nan=True)
+        assert np.array_equal(xo, oxo, equal_nan=True)
+        seen_huge |= bool(np.nanmax(np.abs(x)) > 1e15) if np.isfinite(x).any() else False
+        seen_nan |= bool(np.isnan(x).any())
+    assert seen_huge and seen_nan
+
+
 def test_invalid_arguments_rejected():
     cloth = scenes.grid_cloth(6)
     p = reference_params(3)
