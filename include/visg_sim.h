@@ -65,8 +65,8 @@ typedef struct VisgParams {
     int32_t split_collision; /* 1: collision in its own kernel over the vertices inside a body's
                                 box (default), 0: fused into the step kernel; same results.
                                 visg_batch_autotune may change it.                             */
-    int32_t stage_neighbours; /* 1: each tile's window of neighbour records is staged in shared
-                                memory by TMA bulk copies (default), 0: read from global memory;
+    int32_t stage_neighbours; /* 1: each tile's block of spring entries is staged in shared
+                                memory by TMA bulk copies, 0: read through the L1 (default);
                                 same results.  visg_batch_autotune may change it.              */
     int32_t collision_margin; /* 1: each vertex keeps a proven lower bound of its distance to
                                 every leaf box of its body and skips the first-hit query

@@ -39,9 +39,9 @@ int cuda_fail(cudaError_t e, const char* what) {
     } while (0)
 
 constexpr int kBlocks[3] = {128, 256, 512};
-// largest neighbour window (vertex records) a tile of each block size may stage:
-// two buffers of it stay within 64 / 96 / 128 KB of shared memory
-constexpr int kWindowCap[3] = {1024, 1536, 2048};
+// largest sliced-ELL block (entries) a tile of each block size may stage in shared
+// memory: 16 entries per vertex; two buffers take 32 / 64 / 128 KB
+constexpr int kStageCap[3] = {2048, 4096, 8192};
 int block_index(int b) { return b == 128 ? 0 : (b == 256 ? 1 : (b == 512 ? 2 : -1)); }
 
 struct GarmentIn {
@@ -115,15 +115,15 @@ struct Engine {
     float* d_k = nullptr;
     int4* d_tiles[3] = {nullptr, nullptr, nullptr};
     int n_tiles[3] = {0, 0, 0};
-    int2* d_twin[3] = {nullptr, nullptr, nullptr};  // per tile neighbour window (staged step)
-    int win_cap[3] = {0, 0, 0};                      // records per stage buffer, 0 = no tile staged
+    int2* d_twin[3] = {nullptr, nullptr, nullptr};  // per tile sliced-ELL block {first entry, count}
+    int win_cap[3] = {0, 0, 0};                      // entries per stage buffer, 0 = no tile staged
     uint2* d_sell = nullptr;                         // sliced-ELL springs
     float* d_sellk = nullptr;
     uint32_t* d_slice_off = nullptr;
     uint2* d_vcount = nullptr;                      // springs per list | pin bit, per vertex
     std::vector<uint2> h_vcount;
     uint32_t* d_wild = nullptr;                      // sticky: a record was not tame
-    int stage = 1;                                   // stage neighbour windows (autotuned)
+    int stage = 0;                                   // stage sliced-ELL blocks (autotuned)
     BvhView* d_views = nullptr;
     std::vector<BvhBuffers> bvh;
     int* d_err = nullptr;
@@ -348,26 +348,20 @@ struct Engine {
                     if (perk) sellk[soff[s] + 32 * (int64_t)k + lane] = kk[rp + k];
                 }
             }
-        // tiles for each block size, with the window of vertex records each one's springs touch
+        // tiles for each block size, with the sliced-ELL block of each one's slices
         std::vector<std::vector<int4>> tiles(3);
         std::vector<std::vector<int2>> twin(3);
         for (int b = 0; b < 3; ++b) {
-            const int cap = kWindowCap[b];
+            const int cap = kStageCap[b];
             win_cap[b] = 0;
             for (int g = 0; g < G; ++g)
                 for (int64_t v = voff[g]; v < voff[g + 1]; v += kBlocks[b]) {
                     const int64_t v1 = std::min<int64_t>(v + kBlocks[b], voff[g + 1]);
-                    tiles[b].push_back(make_int4(g, (int)v, (int)v1, (int)(slice0[g] + (v - voff[g]) / 32)));
-                    int64_t lo = v, hi = v1;
-                    for (int64_t u = v; u < v1; ++u)
-                        for (uint32_t e = h_rowp[u] & ROW_MASK; e < (h_rowp[u + 1] & ROW_MASK); ++e) {
-                            const int64_t j = ent[e].x & END_MASK;
-                            lo = std::min(lo, j);
-                            hi = std::max(hi, j + 1);
-                        }
-                    const int64_t cnt = hi - lo;
-                    if (cnt <= cap) {
-                        twin[b].push_back(make_int2((int)lo, (int)cnt));
+                    const int64_t s0 = slice0[g] + (v - voff[g]) / 32, s1 = s0 + (v1 - v + 31) / 32;
+                    tiles[b].push_back(make_int4(g, (int)v, (int)v1, (int)s0));
+                    const int64_t cnt = (int64_t)soff[s1] - soff[s0];
+                    if (cnt > 0 && cnt <= cap && soff[s1] <= 0x7fffffffu) {
+                        twin[b].push_back(make_int2((int)soff[s0], (int)cnt));
                         win_cap[b] = std::max(win_cap[b], (int)cnt);
                     } else {
                         twin[b].push_back(make_int2(0, 0));
@@ -1063,7 +1057,7 @@ void visg_default_params(VisgParams* p) {
     p->max_displacement = 1.0f;
     p->use_graph = 1;
     p->split_collision = 1;
-    p->stage_neighbours = 1;
+    p->stage_neighbours = 0;
     p->collision_margin = 1;
 }
 

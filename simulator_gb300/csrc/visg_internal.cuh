@@ -18,9 +18,9 @@
 //   vcount: uint2 per vertex: the row's springs per list (16 bits each, list 3 15
 //           bits), bit 31 of .y = pinned
 //   tiles:  int4 per tile {garment, first vertex, end vertex, first slice}; a tile
-//           never straddles two garments.  twin: int2 per tile {lo, count}, the
-//           window of vertex records its springs touch (itself included) that a
-//           TMA bulk copy stages in shared memory; count 0 = read from global memory
+//           never straddles two garments.  twin: int2 per tile {first entry, count},
+//           the tile's contiguous sliced-ELL block, which a TMA bulk copy stages in
+//           shared memory; count 0 = read from global memory
 //   per body: LBVH nodes (64 B: both children's boxes and links), leaves (32 B:
 //           v0 and the face normal), root record; build scratch (sort buffers,
 //           look-back status words, handshake flags)
@@ -145,8 +145,8 @@ struct StepArgs {
     const uint32_t* slice_off;
     const uint2* vcount;      // per vertex: springs per list, 16 bits each (list 3: 15), bit 63 = pinned
     uint32_t* wild;           // sticky: some record had |x| or |v| >= 1e15 (or NaN)
-    const int2* twin;         // per tile neighbour window, with SV_STAGED
-    int win_cap;              // records per shared-memory stage buffer
+    const int2* twin;         // per tile sliced-ELL block, with SV_STAGED
+    int win_cap;              // entries per shared-memory stage buffer
     StepParams p;
 };
 
@@ -157,9 +157,9 @@ enum StepVariant : int {
     SV_CHECK = 8,     // divergence check
     SV_KD0 = 16,      // spring damping exactly +0
     SV_SPLIT = 32,    // collision in its own kernel over a compacted candidate list
-    SV_STAGED = 64,   // neighbour windows staged in shared memory by TMA bulk copies
+    SV_STAGED = 64,   // sliced-ELL blocks staged in shared memory by TMA bulk copies
 };
-// dynamic shared memory of a launch: two stage buffers of win_cap records + barriers
+// dynamic shared memory of a launch: two stage buffers of win_cap entries + barriers
 int step_smem_bytes(int variant, int win_cap);
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
 int step_max_ctas_per_sm(int variant, int block, int win_cap);

@@ -3,11 +3,11 @@
 // k_step is the reference's `verlet` kernel (src/verlet.cu:129-161) rebuilt for
 // GB300: one thread per vertex, persistent CTAs walking a tile table (a tile is
 // BLOCK consecutive vertices of one garment, so one launch covers any number of
-// garments of uneven size), 32-byte interleaved state records read with two
-// float4 loads for the vertex and for every spring neighbour (from a window of
-// records that a TMA bulk copy staged in shared memory while the previous tile was
-// computed), springs of all lists merged into one sliced-ELL table of 8-byte
-// entries with the list id in the top bits (no atomics), the previous
+// garments of uneven size), 32-byte interleaved state records (one float4 load per
+// spring neighbour when spring damping is zero, two otherwise), springs of all
+// lists merged into one sliced-ELL table of 8-byte entries (optionally staged per
+// tile in shared memory by TMA bulk copies while the previous tile is computed)
+// summed list by list with the list's stiffness uniform across the loop, the previous
 // contact normal read only for vertices that had a contact, and the collision
 // (collision_response_projection, verlet.cu:24-50) fused behind a warp vote on the
 // body's root box.  Arithmetic follows the reference operation by operation with
@@ -128,29 +128,31 @@ __device__ __forceinline__ f3 spring_force(f3 x, f3 vel, float4 t0, float4 t1, f
     return mul(c, mul(dP, __frcp_rn(dist)));  // normalize(dP) = dP * (1 / |dP|)
 }
 
-// Where a tile's vertex records come from: global memory through the read-only
-// path, or the tile's window [lo, lo + count) staged in shared memory.
+// Vertex records are read through the read-only path (about half the neighbour
+// reads hit L1: rows of a grid share most neighbours).
 struct GlobalRecords {
     const float4* __restrict__ p;
     __device__ __forceinline__ float4 r0(int j) const { return __ldg(p + 2 * j); }
     __device__ __forceinline__ float4 r1(int j) const { return __ldg(p + 2 * j + 1); }
 };
-struct SharedRecords {
-    const float4* p;
-    int lo;
-    __device__ __forceinline__ float4 r0(int j) const { return p[2 * (j - lo)]; }
-    __device__ __forceinline__ float4 r1(int j) const { return p[2 * (j - lo) + 1]; }
+
+// A row's sliced-ELL entries (entry e at p[32 e]): in global memory, or in the tile's
+// block that a TMA bulk copy staged in shared memory.
+template <bool SMEM>
+struct Entries {
+    const uint2* p;
+    __device__ __forceinline__ uint2 operator[](int e) const { return SMEM ? p[32 * e] : __ldg(p + 32 * e); }
 };
 
 // Sum of springs [e, end) of one list of a sliced-ELL row (ep/kp at the row's entry
 // 0, entries 32 apart), in CSR order, two at a time (independent chains).
-template <bool FAST, class Rec>
-__device__ __forceinline__ f3 list_sum(const Rec& rec, const uint2* __restrict__ ep, const float* __restrict__ kp,
-                                       int e, const int end, const float nk, const bool perk, f3 x, f3 vel,
-                                       float kd, f3 eps3) {
+template <bool FAST, class Rec, class Ent>
+__device__ __forceinline__ f3 list_sum(const Rec& rec, const Ent& ep, const float* __restrict__ kp, int e,
+                                       const int end, const float nk, const bool perk, f3 x, f3 vel, float kd,
+                                       f3 eps3) {
     f3 acc = mk3(0.0f, 0.0f, 0.0f);
     for (; e + 1 < end; e += 2) {
-        const uint2 ea = __ldg(ep + 32 * e), eb = __ldg(ep + 32 * (e + 1));
+        const uint2 ea = ep[e], eb = ep[e + 1];
         const int ja = (int)(ea.x & END_MASK), jb = (int)(eb.x & END_MASK);
         const float4 a0 = rec.r0(ja), b0 = rec.r0(jb);
         const float4 a1 = FAST ? a0 : rec.r1(ja), b1 = FAST ? b0 : rec.r1(jb);
@@ -161,7 +163,7 @@ __device__ __forceinline__ f3 list_sum(const Rec& rec, const uint2* __restrict__
         acc = add(add(acc, fa), fb);
     }
     if (e < end) {
-        const uint2 ea = __ldg(ep + 32 * e);
+        const uint2 ea = ep[e];
         const int ja = (int)(ea.x & END_MASK);
         const float4 a0 = rec.r0(ja);
         const float4 a1 = FAST ? a0 : rec.r1(ja);
@@ -173,9 +175,9 @@ __device__ __forceinline__ f3 list_sum(const Rec& rec, const uint2* __restrict__
 
 // F + the spring forces of one vertex, list by list as the reference does
 // (force += list sum, verlet.cu:148-149); cnt holds the row's per-list counts.
-template <bool FAST, class Rec>
-__device__ __forceinline__ f3 row_forces(const Rec& rec, const uint2* __restrict__ ep, const float* __restrict__ kp,
-                                         uint2 cnt, f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
+template <bool FAST, class Rec, class Ent>
+__device__ __forceinline__ f3 row_forces(const Rec& rec, const Ent& ep, const float* __restrict__ kp, uint2 cnt,
+                                         f3 x, f3 vel, f3 F, const StepParams& P, bool perk, f3 eps3) {
     int e = 0;
 #pragma unroll
     for (int l = 0; l < VISG_MAX_LISTS; ++l) {
@@ -201,10 +203,11 @@ __device__ __forceinline__ bool tame(f3 x, f3 v) {
 // v = (x - x_old) / dt.  x_old is x itself when FLAG_XO_IS_X is set (after a
 // contact, a pin or update_vertex) and otherwise the previous step's x, which is
 // still in the other buffer: the step reads it there before overwriting it.
-template <bool COLL, bool KD0, bool SPLIT, class Rec>
-__device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, const int4 td, const int refv,
-                                            const int check, const int perk, const bool wild, float& my_disp,
-                                            uint32_t& my_bad) {
+template <bool COLL, bool KD0, bool SPLIT, bool SMEM_ENT>
+__device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, const uint2* ebase, const uint32_t e0,
+                                            const int refv, const int check, const int perk, const bool wild,
+                                            float& my_disp, uint32_t& my_bad) {
+    const GlobalRecords rec{a.state_in};
     const StepParams& P = a.p;
     const f3 grav = mk3(P.gx, P.gy, P.gz);
     const f3 eps3 = mk3(kFltEpsilon, kFltEpsilon, kFltEpsilon);
@@ -222,12 +225,12 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const Rec& rec, c
     bool has_n = false;
     if (active && !pinned) {
         const int lane = (int)(threadIdx.x & 31u);
-        const uint32_t sb = __ldg(&a.slice_off[td.w + (int)(threadIdx.x >> 5)]) + (uint32_t)lane;
+        const uint32_t sb = __ldg(&a.slice_off[td.w + (int)(threadIdx.x >> 5)]) + (uint32_t)lane;  // row entry 0
         const f3 xo = (flags & FLAG_XO_IS_X) ? x : xyz(a.state_out[2 * ii]);
         f3 np = mk3(0.0f, 0.0f, 0.0f);
         if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
         const f3 F0 = add(mul(grav, P.mass), mul(vel, P.damp));
-        const uint2* ep = a.sell + sb;
+        const Entries<SMEM_ENT> ep{ebase + (sb - e0)};
         const float* kp = perk ? a.sellk + sb : nullptr;
         f3 F;
         if (KD0) {
@@ -373,49 +376,50 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return true;
 }
 
-// thread 0: stage the window of `tile` (if it has one) into buffer `b`
-__device__ __forceinline__ void stage_window(const StepArgs& a, int tile, uint32_t win, uint32_t bar) {
+// thread 0: stage the sliced-ELL block of `tile` (if it has one) at shared address dst
+__device__ __forceinline__ void stage_entries(const StepArgs& a, int tile, uint32_t dst, uint32_t bar) {
     const int2 tw = __ldg(&a.twin[tile]);
     if (tw.y > 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the buffer come first
-        bulk_stage(win, a.state_in + 2 * (size_t)tw.x, (uint32_t)tw.y * 32u, bar);
+        bulk_stage(dst, a.sell + (uint32_t)tw.x, (uint32_t)tw.y * 8u, bar);
     }
 }
 
 // The fused step: persistent CTAs walk the tile table.  With STAGED, thread 0 copies
-// the next tile's window of vertex records (a contiguous run of 32-byte records,
-// usually the tile and a band of rows either side) into the other shared-memory
-// buffer with one TMA bulk copy while the CTA computes the current tile, so the
-// spring gathers hit shared memory; tiles whose window exceeds the buffer read
-// global memory.  Waits are bounded: a copy that has not landed after kWaitNs sets
-// ERR_TIMEOUT, and the CTA waits (again bounded) for its copies in flight and exits.
+// the next tile's block of sliced-ELL entries (the tile's slices are contiguous: one
+// TMA bulk copy) into the other shared-memory buffer while the CTA computes the
+// current tile, so each spring's chain starts with a shared-memory load; tiles whose
+// block exceeds the buffer read their entries from global memory.  Waits are bounded:
+// a copy that has not landed after kWaitNs sets ERR_TIMEOUT, and the CTA waits (again
+// bounded) for its copies in flight and exits.
 template <int BLOCK, bool COLL, bool KD0, bool SPLIT, bool STAGED>
 __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
     extern __shared__ __align__(128) unsigned char dyn_smem[];
     float my_disp = 0.0f;
     uint32_t my_bad = 0;
-    const GlobalRecords grec{a.state_in};
     const bool wild = *reinterpret_cast<const volatile uint32_t*>(a.wild) != 0u;
     if (!STAGED) {
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x)
-            vertex_step<COLL, KD0, SPLIT>(a, grec, __ldg(&a.tiles[tile]), refv, check, perk, wild, my_disp, my_bad);
+            vertex_step<COLL, KD0, SPLIT, false>(a, __ldg(&a.tiles[tile]), a.sell, 0u, refv, check, perk, wild,
+                                                 my_disp, my_bad);
     } else {
         const uint32_t bar = smem_addr(dyn_smem);
-        const uint32_t win = bar + kBarBytes;
-        const float4* swin = reinterpret_cast<const float4*>(dyn_smem + kBarBytes);
-        const uint32_t wbytes = (uint32_t)a.win_cap * 32u;
+        const uint32_t buf0 = bar + kBarBytes;
+        const uint2* sbuf = reinterpret_cast<const uint2*>(dyn_smem + kBarBytes);
+        const uint32_t bbytes = (uint32_t)a.win_cap * 8u;
         if (threadIdx.x == 0) {
             mbar_init(bar);
             mbar_init(bar + 8);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         __syncthreads();
-        if (threadIdx.x == 0 && (int)blockIdx.x < a.n_tiles) stage_window(a, blockIdx.x, win, bar);
+        if (threadIdx.x == 0 && (int)blockIdx.x < a.n_tiles) stage_entries(a, blockIdx.x, buf0, bar);
         uint32_t par = 0;  // parity of the next phase of each buffer's barrier
         int b = 0;
         for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, b ^= 1) {
             const int nxt = tile + (int)gridDim.x;
-            if (threadIdx.x == 0 && nxt < a.n_tiles) stage_window(a, nxt, win + (uint32_t)(b ^ 1) * wbytes, bar + 8u * (b ^ 1));
+            if (threadIdx.x == 0 && nxt < a.n_tiles)
+                stage_entries(a, nxt, buf0 + (uint32_t)(b ^ 1) * bbytes, bar + 8u * (b ^ 1));
             const int4 td = __ldg(&a.tiles[tile]);
             const int2 tw = __ldg(&a.twin[tile]);
             bool ok = true;
@@ -423,10 +427,10 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
                 ok = __all_sync(0xffffffffu, mbar_wait(bar + 8u * b, (par >> b) & 1u));
                 par ^= 1u << b;
                 if (ok)
-                    vertex_step<COLL, KD0, SPLIT>(a, SharedRecords{swin + 2 * b * a.win_cap, tw.x}, td, refv, check,
-                                                  perk, wild, my_disp, my_bad);
+                    vertex_step<COLL, KD0, SPLIT, true>(a, td, sbuf + (size_t)b * a.win_cap, (uint32_t)tw.x, refv,
+                                                        check, perk, wild, my_disp, my_bad);
             } else {
-                vertex_step<COLL, KD0, SPLIT>(a, grec, td, refv, check, perk, wild, my_disp, my_bad);
+                vertex_step<COLL, KD0, SPLIT, false>(a, td, a.sell, 0u, refv, check, perk, wild, my_disp, my_bad);
             }
             if (__syncthreads_or(!ok)) {
                 // a copy did not land: record it, let this CTA's copies in flight finish, leave
@@ -704,7 +708,7 @@ cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cud
 }
 
 int step_smem_bytes(int variant, int win_cap) {
-    return (variant & SV_STAGED) ? kBarBytes + 2 * 32 * win_cap : 0;
+    return (variant & SV_STAGED) ? kBarBytes + 2 * 8 * win_cap : 0;
 }
 
 int step_max_ctas_per_sm(int variant, int block, int win_cap) {

@@ -54,7 +54,7 @@ def reference_params(n_lists: int = 2) -> VisgParams:
     p.max_displacement = 1.0
     p.use_graph = 1
     p.split_collision = 1
-    p.stage_neighbours = 1
+    p.stage_neighbours = 0
     p.collision_margin = 1
     return p
 
@@ -62,7 +62,7 @@ def reference_params(n_lists: int = 2) -> VisgParams:
 def make_params(n_lists: int, dt: float, mass: float, gravity=(0.0, -9.8, 0.0), force_damping=0.0,
                 spring_damping=0.0, verlet_damping=1.0, thickness=0.003, box_depth=0.01,
                 list_k=(100.0, 2.0, 2.0, 2.0), collide=1, check_every=0, max_displacement=1.0,
-                use_graph=1, split_collision=1, stage_neighbours=1,
+                use_graph=1, split_collision=1, stage_neighbours=0,
                 collision_margin=1) -> VisgParams:
     p = VisgParams()
     p.dt, p.mass = dt, mass
