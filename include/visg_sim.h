@@ -68,10 +68,12 @@ typedef struct VisgParams {
     int32_t stage_neighbours; /* 1: each tile's block of spring entries is staged in shared
                                 memory by TMA bulk copies, 0: read through the L1 (default);
                                 same results.  visg_batch_autotune may change it.              */
-    int32_t collision_margin; /* 1: each vertex keeps a proven lower bound of its distance to
-                                every leaf box of its body and skips the first-hit query
-                                while it has moved less than that (default); 0: query every
-                                step.  Same results; update_body clears the bounds.        */
+    int32_t collision_margin; /* 1: each vertex caches its last first-hit query's answer with
+                                a margin (how far it may move before any box the query
+                                tested could answer differently) and reuses the answer
+                                while it stays within it, redoing only the plane test
+                                (default); 0: query every step.  Same results;
+                                update_body clears the caches.                           */
 } VisgParams;
 
 void visg_default_params(VisgParams* p);
@@ -229,6 +231,9 @@ int visg_batch_set_stream(VisgBatch* b, void* cuda_stream);
 int visg_batch_step(VisgBatch* b, int32_t nsteps);
 /* garment = -1: all garments concatenated in id order. */
 int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device);
+/* visg_get_state / visg_set_state of one garment (garment = -1: all, concatenated). */
+int visg_batch_get_state(VisgBatch* b, int32_t garment, float* x, float* x_old, float* normal);
+int visg_batch_set_state(VisgBatch* b, int32_t garment, const float* x, const float* x_old, const float* normal);
 /* visg_read_positions_async / visg_wait_positions over all garments (concatenated). */
 int visg_batch_read_positions_async(VisgBatch* b, float* out);
 int visg_batch_wait_positions(VisgBatch* b);

@@ -86,6 +86,8 @@ def lib():
         "visg_batch_autotune": (C.c_int, [_vp, _i32p, _i32p]),
         "visg_batch_set_launch": (C.c_int, [_vp, C.c_int32, C.c_int32]),
         "visg_batch_read_positions_async": (C.c_int, [_vp, _vp]),
+        "visg_batch_get_state": (C.c_int, [_vp, C.c_int32, _fp, _fp, _fp]),
+        "visg_batch_set_state": (C.c_int, [_vp, C.c_int32, _fp, _fp, _fp]),
         "visg_batch_wait_positions": (C.c_int, [_vp]),
         "visg_read_positions_async": (C.c_int, [_vp, _vp]),
         "visg_wait_positions": (C.c_int, [_vp]),
@@ -353,6 +355,15 @@ class BatchSimulator:
         b, c = C.c_int32(), C.c_int32()
         _check(lib().visg_batch_autotune(self.h, C.byref(b), C.byref(c)))
         return b.value, c.value
+
+    def state(self, garment: int = -1):
+        n = int(self.offsets[-1]) if garment < 0 else self.sizes[garment]
+        x, xo, nr = (np.empty((n, 3), np.float32) for _ in range(3))
+        _check(lib().visg_batch_get_state(self.h, garment, _p(x), _p(xo), _p(nr)))
+        return x, xo, nr
+
+    def set_state(self, garment: int = -1, x=None, xo=None, n=None):
+        _check(lib().visg_batch_set_state(self.h, garment, _p(_f32(x)), _p(_f32(xo)), _p(_f32(n))))
 
     def set_launch(self, block: int, ctas_per_sm: int):
         _check(lib().visg_batch_set_launch(self.h, block, ctas_per_sm))

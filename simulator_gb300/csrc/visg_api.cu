@@ -130,6 +130,7 @@ struct Engine {
     uint32_t* d_check = nullptr;
     int2* d_cand = nullptr;            // split collision: queued candidates
     uint32_t* d_cand_count = nullptr;
+    int* d_hitleaf = nullptr;          // query cache: first-hit leaf per vertex
     int split = 1;                     // collision in its own kernel (autotuned)
     float* d_stage = nullptr;  // 9*N floats
     uint32_t* h_status = nullptr;  // pinned: err, check0, check1
@@ -390,6 +391,7 @@ struct Engine {
         arena.want(&d_check, 4);
         arena.want(&d_cand, (size_t)N + 1);
         arena.want(&d_cand_count, 4);
+        arena.want(&d_hitleaf, (size_t)N + 1);
         arena.want(&d_stage, 9 * (size_t)N + 4);
         bvh.resize(G);
         for (int g = 0; g < G; ++g)
@@ -498,6 +500,7 @@ struct Engine {
         a.check = d_check;
         a.cand = d_cand;
         a.cand_count = d_cand_count;
+        a.hitleaf = d_hitleaf;
         a.sell = d_sell;
         a.sellk = d_sellk;
         a.slice_off = d_slice_off;
@@ -758,28 +761,44 @@ struct Engine {
         return sync();
     }
 
-    int get_state(float* x, float* xo, float* nrm) {
+    // vertex range of garment g (g = -1: all garments)
+    int garment_range(int g, int64_t& v0, int64_t& n) const {
+        v0 = 0;
+        n = N;
+        if (g < 0) return VISG_OK;
+        if (g >= G) return fail(VISG_ERR_INVALID_ARG, "garment out of range");
+        v0 = voff[g];
+        n = voff[g + 1] - voff[g];
+        return VISG_OK;
+    }
+
+    int get_state(int g, float* x, float* xo, float* nrm) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        int64_t v0, n;
+        if (int r = garment_range(g, v0, n)) return r;
         float* sx = d_stage;
-        float* sxo = d_stage + 3 * N;
-        float* sn = d_stage + 6 * N;
-        CU(launch_unpack_state(d_state[cur], d_state[cur ^ 1], d_normal, N, sx, sxo, sn, stream));
-        if (x) CU(cudaMemcpyAsync(x, sx, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
-        if (xo) CU(cudaMemcpyAsync(xo, sxo, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
-        if (nrm) CU(cudaMemcpyAsync(nrm, sn, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
+        float* sxo = d_stage + 3 * n;
+        float* sn = d_stage + 6 * n;
+        CU(launch_unpack_state(d_state[cur] + 2 * v0, d_state[cur ^ 1] + 2 * v0, d_normal + v0, n, sx, sxo, sn,
+                               stream));
+        if (x) CU(cudaMemcpyAsync(x, sx, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
+        if (xo) CU(cudaMemcpyAsync(xo, sxo, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
+        if (nrm) CU(cudaMemcpyAsync(nrm, sn, (size_t)n * 12, cudaMemcpyDeviceToHost, stream));
         return sync();
     }
 
-    int set_state(const float* x, const float* xo, const float* nrm) {
+    int set_state(int g, const float* x, const float* xo, const float* nrm) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        int64_t v0, n;
+        if (int r = garment_range(g, v0, n)) return r;
         float* sx = d_stage;
-        float* sxo = d_stage + 3 * N;
-        float* sn = d_stage + 6 * N;
-        if (x) CU(cudaMemcpyAsync(sx, x, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
-        if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
-        if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)N * 12, cudaMemcpyHostToDevice, stream));
-        CU(launch_pack_state(d_state[cur], d_state[cur ^ 1], d_normal, N, x ? sx : nullptr, xo ? sxo : nullptr,
-                             nrm ? sn : nullptr, p.dt, d_wild, stream));
+        float* sxo = d_stage + 3 * n;
+        float* sn = d_stage + 6 * n;
+        if (x) CU(cudaMemcpyAsync(sx, x, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
+        if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
+        if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
+        CU(launch_pack_state(d_state[cur] + 2 * v0, d_state[cur ^ 1] + 2 * v0, d_normal + v0, n, x ? sx : nullptr,
+                             xo ? sxo : nullptr, nrm ? sn : nullptr, p.dt, d_wild, stream));
         CU(cudaStreamSynchronize(stream));
         return VISG_OK;
     }
@@ -949,6 +968,8 @@ struct Engine {
                                     cudaMemcpyDeviceToDevice, stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(d_normal, bn, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
+            // the query caches refer to hitleaf, which the timed steps overwrote
+            if (e == cudaSuccess) e = launch_clear_margin(d_state[cur], 0, N, stream);
         };
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
@@ -1153,12 +1174,12 @@ int visg_wait_positions(VisgSim* sim) {
 
 int visg_get_state(VisgSim* sim, float* x, float* xo, float* n) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
-    return sim->eng.get_state(x, xo, n);
+    return sim->eng.get_state(-1, x, xo, n);
 }
 
 int visg_set_state(VisgSim* sim, const float* x, const float* xo, const float* n) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
-    return sim->eng.set_state(x, xo, n);
+    return sim->eng.set_state(-1, x, xo, n);
 }
 
 int visg_sync(VisgSim* sim) {
@@ -1260,6 +1281,16 @@ int visg_batch_step(VisgBatch* b, int32_t nsteps) {
 int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.get_positions(garment, out, on_device);
+}
+
+int visg_batch_get_state(VisgBatch* b, int32_t garment, float* x, float* x_old, float* normal) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.get_state(garment, x, x_old, normal);
+}
+
+int visg_batch_set_state(VisgBatch* b, int32_t garment, const float* x, const float* x_old, const float* normal) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.set_state(garment, x, x_old, normal);
 }
 
 int visg_batch_read_positions_async(VisgBatch* b, float* out) {

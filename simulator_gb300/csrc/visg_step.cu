@@ -38,15 +38,6 @@ __device__ __forceinline__ bool in_box(f3 p, float4 lo, float4 hi) {  // BBox::i
     return (p.x >= lo.x && p.x <= hi.x) && (p.y >= lo.y && p.y <= hi.y) && (p.z >= lo.z && p.z <= hi.z);
 }
 
-// Lower bound of the L-infinity distance from p to the closed box [lo, hi]: the
-// largest per-axis gap, each rounded down (0 or less when p is inside).
-__device__ __forceinline__ float box_gap(f3 p, float4 lo, float4 hi) {
-    const float gx = fmaxf(__fsub_rd(lo.x, p.x), __fsub_rd(p.x, hi.x));
-    const float gy = fmaxf(__fsub_rd(lo.y, p.y), __fsub_rd(p.y, hi.y));
-    const float gz = fmaxf(__fsub_rd(lo.z, p.z), __fsub_rd(p.z, hi.z));
-    return fmaxf(gx, fmaxf(gy, gz));
-}
-
 // Upper bound of max_axis |a - b| (each difference rounded up).
 __device__ __forceinline__ float disp_bound(f3 a, f3 b) {
     const float dx = __fsub_ru(fmaxf(a.x, b.x), fminf(a.x, b.x));
@@ -55,22 +46,36 @@ __device__ __forceinline__ float disp_bound(f3 a, f3 b) {
     return fmaxf(dx, fmaxf(dy, dz));
 }
 
+// Lower bounds (differences rounded down) of the L-infinity distance p can move
+// before the closed-box test (BBox::intersect) changes its answer: outside the box,
+// the largest per-axis gap; inside, the distance to the nearest face.
+__device__ __forceinline__ float box_gap(f3 p, float4 lo, float4 hi) {
+    return fmaxf(fmaxf(fmaxf(__fsub_rd(lo.x, p.x), __fsub_rd(p.x, hi.x)), fmaxf(__fsub_rd(lo.y, p.y), __fsub_rd(p.y, hi.y))),
+                 fmaxf(__fsub_rd(lo.z, p.z), __fsub_rd(p.z, hi.z)));
+}
+__device__ __forceinline__ float box_inner(f3 p, float4 lo, float4 hi) {
+    return fminf(fminf(fminf(__fsub_rd(p.x, lo.x), __fsub_rd(hi.x, p.x)), fminf(__fsub_rd(p.y, lo.y), __fsub_rd(hi.y, p.y))),
+                 fminf(__fsub_rd(p.z, lo.z), __fsub_rd(hi.z, p.z)));
+}
+
 // D_BVH::intersect semantics: children tested pairwise; an overlapping leaf child is
 // returned before any descent (A before B); both internal -> descend A, push B.
-// A depth-first walk visits every internal node at most once, so `budget` (the
-// number of internal nodes) bounds the loop even on a corrupted tree.
-// With GAP, a query that finds no leaf also returns in `gap` a lower bound of the
-// distance from p to every leaf box: every leaf lies under a child box the walk
-// rejected, and a node's box contains its children's boxes.
-template <bool GAP>
+// The answer is therefore the first leaf, in a fixed order of the tree's leaves,
+// whose box contains p (a node's box contains its children's).  A depth-first walk
+// visits every internal node at most once, so `budget` (the number of internal
+// nodes) bounds the loop even on a corrupted tree.
+// With MARGIN, m receives a distance a point may move from p and keep the answer:
+// every leaf before the answer lies under a box the walk rejected (min of their
+// gaps), and the answer's own box must keep containing it (its inner distance).
+template <bool MARGIN>
 __device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int node, int budget, f3 p, int* err,
-                                         float& gap) {
+                                         float& m) {
     int stack[kStack];
     int sp = 0;
     while (true) {
         if (--budget < 0) {
             atomicOr(err, ERR_STACK);
-            gap = 0.0f;
+            m = 0.0f;
             return -1;
         }
         const Node* nd = nodes + node;
@@ -78,12 +83,16 @@ __device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int nod
         const float4 blo = __ldg(&nd->b_lo), bhi = __ldg(&nd->b_hi);
         const int la = __float_as_int(alo.w), lb = __float_as_int(blo.w);
         const bool ol = in_box(p, alo, ahi), orr = in_box(p, blo, bhi);
-        if (ol && la < 0) return ~la;
-        if (orr && lb < 0) return ~lb;
-        if (GAP) {
-            if (!ol) gap = fminf(gap, box_gap(p, alo, ahi));
-            if (!orr) gap = fminf(gap, box_gap(p, blo, bhi));
+        if (ol && la < 0) {
+            if (MARGIN) m = fminf(m, box_inner(p, alo, ahi));
+            return ~la;
         }
+        if (MARGIN && !ol) m = fminf(m, box_gap(p, alo, ahi));
+        if (orr && lb < 0) {
+            if (MARGIN) m = fminf(m, box_inner(p, blo, bhi));
+            return ~lb;
+        }
+        if (MARGIN && !orr) m = fminf(m, box_gap(p, blo, bhi));
         const bool tl = ol && la >= 0, tr = orr && lb >= 0;
         if (!tl && !tr) {
             if (sp == 0) return -1;
@@ -93,7 +102,7 @@ __device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int nod
             if (tl && tr) {
                 if (sp == kStack) {
                     atomicOr(err, ERR_STACK);
-                    gap = 0.0f;
+                    m = 0.0f;
                     return -1;
                 }
                 stack[sp++] = lb;
@@ -102,12 +111,27 @@ __device__ __forceinline__ int first_hit(const Node* __restrict__ nodes, int nod
     }
 }
 
+// The whole first-hit query of one body (root box, single leaf, walk) with its margin.
+__device__ __forceinline__ int query_margin(const BvhView& bv, f3 p, int* err, float& m) {
+    const int nl = bv.root->n_leaves;
+    const float4 lo = bv.root->top_lo, hi = bv.root->top_hi;
+    if (!in_box(p, lo, hi)) {
+        m = fminf(m, box_gap(p, lo, hi));
+        return -1;
+    }
+    if (nl == 1) {
+        m = fminf(m, box_inner(p, lo, hi));
+        return 0;
+    }
+    return first_hit<true>(bv.nodes, bv.root->root, nl, p, err, m);
+}
+
 __device__ __forceinline__ int query_leaf(const BvhView& bv, int n_leaves, int root, float4 top_lo, float4 top_hi,
                                           f3 p, int* err) {
     if (n_leaves <= 0 || !in_box(p, top_lo, top_hi)) return -1;
     if (n_leaves == 1) return 0;
-    float gap = 0.0f;
-    return first_hit<false>(bv.nodes, root, n_leaves, p, err, gap);
+    float m = 0.0f;
+    return first_hit<false>(bv.nodes, root, n_leaves, p, err, m);
 }
 
 // Force of one spring on the vertex at x moving with velocity vel (verlet.cu:64-84):
@@ -252,61 +276,62 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
         else xn = add(add(x, mul(P.gamma, sub(x, xo))), adt);
         xon = x;
     }
-    // Collision margin: s1.w holds a lower bound of the distance from x to every leaf
-    // box of the body, proven by the last query that found no leaf.  While the vertex
-    // has moved less than that since, the query would find no leaf again and is
-    // skipped; the bound shrinks by each step's displacement (rounded up).
+    // Query cache.  s1.w holds a margin: while the vertex stays within that L-infinity
+    // distance of the point its last first-hit query was answered at, the query's
+    // answer is unchanged (first_hit's margin) and is reused: no leaf, or the leaf in
+    // hitleaf (FLAG_LEAF_CACHED), whose plane test is redone at the new position.
+    // The margin shrinks by every displacement since (rounded up); 0 = no cache.
     float skin = 0.0f;
-    bool far = false;
-    if (COLL && P.margin && active && !pinned) {
-        skin = __fsub_rd(s1.w, disp_bound(xn, x));
-        far = skin > 0.0f;
-    }
-    if (COLL && SPLIT) {
-        // split collision: queue the vertices inside their body's box (one atomic per
-        // warp); k_collide traverses them with fully populated warps
+    bool cached = false;  // the stored margin refers to hitleaf[i]
+    if (COLL) {
         const BvhView bv = a.bodies[td.x];
-        bool cand = false;
-        if (bv.root != nullptr)
-            cand = active && !pinned && bv.root->n_leaves > 0 && in_box(xn, bv.root->top_lo, bv.root->top_hi);
-        if (!cand) skin = 0.0f;
-        cand = cand && !far;
-        if (cand) skin = 0.0f;  // k_collide stores the new bound
-        const unsigned m = __ballot_sync(0xffffffffu, cand);
-        if (m) {
-            const int lane = (int)(threadIdx.x & 31u), leader = __ffs(m) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(a.cand_count, (uint32_t)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (cand) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, td.x);
-        }
-    } else if (COLL) {
-        const BvhView bv = a.bodies[td.x];
-        if (bv.root != nullptr) {
-            const int nl = bv.root->n_leaves;
-            const int rt = bv.root->root;
-            const float4 tlo = bv.root->top_lo, thi = bv.root->top_hi;
-            bool cand = active && !pinned && nl > 0 && in_box(xn, tlo, thi);
-            if (!cand) skin = 0.0f;
-            cand = cand && !far;
-            if (__any_sync(0xffffffffu, cand)) {
-                if (cand) {
-                    float gap = __int_as_float(0x7f800000);  // +inf
-                    const int leaf = nl == 1 ? 0 : first_hit<true>(bv.nodes, rt, nl, xn, a.err, gap);
-                    skin = (leaf < 0 && P.margin) ? gap : 0.0f;
-                    if (leaf >= 0) {
-                        const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
-                        const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
-                        const f3 n = mk3(L0.w, L1.x, L1.y);
-                        const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), n);
-                        if (!(d > 0.0f)) {
-                            xn = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), n));
-                            xon = xn;
-                            nn = n;
-                            has_n = true;
-                        }
-                    }
+        const bool body = bv.root != nullptr && bv.root->n_leaves > 0;
+        bool query = false;
+        int leaf = -1;
+        if (body && active && !pinned) {
+            const float rem = P.margin ? __fsub_rd(s1.w, disp_bound(xn, x)) : 0.0f;
+            if (rem > 0.0f) {
+                skin = rem;
+                if (flags & FLAG_LEAF_CACHED) {
+                    leaf = __ldg(&a.hitleaf[ii]);
+                    cached = true;
                 }
+            } else {
+                query = true;
+            }
+        }
+        if (SPLIT) {
+            // queue the queries (one atomic per warp); k_collide answers them with fully
+            // populated warps and stores their margins
+            const unsigned m = __ballot_sync(0xffffffffu, query);
+            if (m) {
+                const int lane = (int)(threadIdx.x & 31u), leader = __ffs(m) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(a.cand_count, (uint32_t)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (query) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, td.x);
+            }
+        } else if (__any_sync(0xffffffffu, query) && query) {
+            float m = __int_as_float(0x7f800000);  // +inf
+            leaf = query_margin(bv, xn, a.err, m);
+            if (P.margin) {
+                skin = m;
+                cached = leaf >= 0;
+                if (cached) a.hitleaf[i] = leaf;
+            }
+        }
+        if (leaf >= 0) {  // plane test of the first-hit leaf (primitive.cu:110-125)
+            const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
+            const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
+            const f3 n = mk3(L0.w, L1.x, L1.y);
+            const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), n);
+            if (!(d > 0.0f)) {
+                const f3 xp = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), n));
+                skin = __fsub_rd(skin, disp_bound(xp, xn));
+                xn = xp;
+                xon = xn;
+                nn = n;
+                has_n = true;
             }
         }
     }
@@ -315,7 +340,8 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
         const bool xo_is_x = pinned || has_n;
         const f3 vn = divs(sub(xn, xon), P.dt);
         untamed = !tame(xn, vn);
-        const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u);
+        const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u) |
+                            (cached && skin > 0.0f ? FLAG_LEAF_CACHED : 0u);
         a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, vn.x);
         a.state_out[2 * i + 1] = make_float4(vn.y, vn.z, __uint_as_float(fl), skin > 0.0f ? skin : 0.0f);
         if (has_n) a.normal[i] = make_float4(nn.x, nn.y, nn.z, 0.0f);
@@ -456,10 +482,11 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
     }
 }
 
-// Split collision (collision_response_projection, verlet.cu:24-50) over the queued
-// candidates: the integrate pass has already written every vertex's record as if
-// it had no contact; a projected vertex gets x' += |dist| n, x_old' = x', v' = 0
-// and its normal.
+// Split collision (collision_response_projection, verlet.cu:24-50): the queued
+// first-hit queries.  The integrate pass has already written each record as if it
+// had no contact (flags without a cache, margin 0); a projected vertex gets
+// x' += |dist| n, x_old' = x', v' = 0 and its normal; every answered query stores its
+// margin (and leaf) for the query cache.
 constexpr int COLLIDE_BLOCK = 256;
 __global__ void __launch_bounds__(COLLIDE_BLOCK) k_collide(const StepArgs a) {
     const uint32_t n = *a.cand_count;
@@ -467,27 +494,40 @@ __global__ void __launch_bounds__(COLLIDE_BLOCK) k_collide(const StepArgs a) {
     for (uint32_t k = blockIdx.x * COLLIDE_BLOCK + threadIdx.x; k < n; k += gridDim.x * COLLIDE_BLOCK) {
         const int2 c = a.cand[k];
         const BvhView bv = a.bodies[c.y];
-        const int nl = bv.root->n_leaves;
-        const float4 s0 = a.state_out[2 * c.x];
+        float4 s0 = a.state_out[2 * c.x], s1 = a.state_out[2 * c.x + 1];
         f3 xn = mk3(s0.x, s0.y, s0.z);
-        float gap = __int_as_float(0x7f800000);  // +inf
-        const int leaf = nl == 1 ? 0 : first_hit<true>(bv.nodes, bv.root->root, nl, xn, a.err, gap);
-        if (leaf < 0) {
-            if (a.p.margin) reinterpret_cast<float*>(a.state_out + 2 * c.x + 1)[3] = gap;  // the record's w
-            continue;
+        float m = __int_as_float(0x7f800000);  // +inf
+        const int leaf = query_margin(bv, xn, a.err, m);
+        uint32_t fl = __float_as_uint(s1.z);
+        float skin = a.p.margin ? m : 0.0f;
+        if (leaf >= 0) {
+            if (a.p.margin) {
+                a.hitleaf[c.x] = leaf;
+                fl |= FLAG_LEAF_CACHED;
+            }
+            const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
+            const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
+            const f3 nrm = mk3(L0.w, L1.x, L1.y);
+            const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), nrm);
+            if (!(d > 0.0f)) {
+                const f3 xp = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), nrm));
+                skin = __fsub_rd(skin, disp_bound(xp, xn));
+                xn = xp;
+                const f3 vn = divs(sub(xn, xn), dt);
+                s0 = make_float4(xn.x, xn.y, xn.z, vn.x);
+                s1.x = vn.y;
+                s1.y = vn.z;
+                fl |= FLAG_HAS_NORMAL | FLAG_XO_IS_X;
+                a.state_out[2 * c.x] = s0;
+                a.normal[c.x] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+                if (!tame(xn, vn)) atomicOr(a.wild, 1u);
+            }
         }
-        const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
-        const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
-        const f3 nrm = mk3(L0.w, L1.x, L1.y);
-        const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), nrm);
-        if (d > 0.0f) continue;
-        xn = add(xn, mul(__fmul_rn(1.0f, fabsf(d)), nrm));
-        const f3 vn = divs(sub(xn, xn), dt);
-        a.state_out[2 * c.x] = make_float4(xn.x, xn.y, xn.z, vn.x);
-        a.state_out[2 * c.x + 1] =
-            make_float4(vn.y, vn.z, __uint_as_float(FLAG_HAS_NORMAL | FLAG_XO_IS_X), 0.0f);
-        a.normal[c.x] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
-        if (!tame(xn, vn)) atomicOr(a.wild, 1u);
+        if (!(skin > 0.0f)) {
+            skin = 0.0f;
+            fl &= ~FLAG_LEAF_CACHED;
+        }
+        a.state_out[2 * c.x + 1] = make_float4(s1.x, s1.y, __uint_as_float(fl), skin);
     }
 }
 

@@ -263,11 +263,14 @@ def sheet_over_sphere(side: int = 64, subdiv: int = 4, radius: float = 0.3, seed
 
 
 def garment_batch(n_garments: int = 256, seed: int = 0, side_range=(32, 256), subdiv_range=(3, 6),
-                  radius_range=(0.2, 0.4), cap: float = 0.05):
+                  radius_range=(0.2, 0.4), centre_depth: float = 0.5, cap: float | None = None,
+                  pin_corners: bool = True):
     """Per garment: side ~ U{32..256}, a 1 m sheet with the three spring families and
     two pinned corners, facing an icosphere of subdivision ~ U{3..6} and radius
-    ~ U[0.2, 0.4] m whose top rises `cap` metres through the sheet (the sheet starts
-    draped over the sphere's cap, so the collision path is exercised from step 1)."""
+    ~ U[0.2, 0.4] m centred `centre_depth` metres below the sheet (the single-sheet
+    workload's placement); the sheet falls onto it.  With `cap`, the sphere's top
+    instead rises `cap` metres through the sheet (cap > 0 starts with a deep overlap
+    that the first step projects out: violent, and unstable at these stiffnesses)."""
     rng = np.random.default_rng(seed)
     sides = rng.integers(side_range[0], side_range[1] + 1, size=n_garments)
     subs = rng.integers(subdiv_range[0], subdiv_range[1] + 1, size=n_garments)
@@ -275,13 +278,14 @@ def garment_batch(n_garments: int = 256, seed: int = 0, side_range=(32, 256), su
     spheres = {}
     out = []
     for g in range(n_garments):
-        cloth = grid_cloth(int(sides[g]), 1.0, 0.0)
+        cloth = grid_cloth(int(sides[g]), 1.0, 0.0, pin_top_corners=pin_corners)
         key = int(subs[g])
         if key not in spheres:
             spheres[key] = icosphere(key, 1.0)
         unit = spheres[key]
         r = float(radii[g])
-        body = Body(xyz=(unit.xyz.astype(np.float64) * r + np.array([0.0, cap - r, 0.0])).astype(np.float32),
+        cy = -centre_depth if cap is None else cap - r
+        body = Body(xyz=(unit.xyz.astype(np.float64) * r + np.array([0.0, cy, 0.0])).astype(np.float32),
                     tris=unit.tris, normals=unit.normals)
         out.append((cloth, body))
     return out

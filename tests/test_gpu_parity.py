@@ -412,6 +412,28 @@ def test_batch_pipelined_reads():
         assert np.array_equal(got[k % 2], b.positions())
 
 
+def test_batch_state_per_garment():
+    cloth, cl, body, p = ref_scene(side=20, subdiv=2)
+    b = vs.BatchSimulator(p)
+    for _ in range(3):
+        b.add(cloth.xyz, cl, body.xyz, body.tris, body.normals)
+    b.finalize()
+    b.step(30)
+    x, xo, n = b.state(1)
+    s = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    s.set_state(x, xo, n)
+    for u, v in zip(s.state(), (x, xo, n)):
+        assert np.array_equal(u, v)
+    b.step(10)
+    s.simulate(10)
+    assert np.array_equal(b.positions(1), s.positions())
+    b.set_state(2, *s.state())  # garment 2 takes the plain simulator's state
+    b.step(5)
+    s.simulate(5)
+    assert np.array_equal(b.positions(2), s.positions())
+    assert np.array_equal(b.state(-1)[0], b.positions())
+
+
 def test_batch_autotune_keeps_state_and_results():
     p = reference_params(3)
     items = [(scenes.grid_cloth(s, 1.0, 0.0), scenes.icosphere(2, 0.3, (0, -0.3, 0))) for s in (30, 50, 70)]
