@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--launch", default=None, help="block,ctas_per_sm instead of autotuning (profiling runs)")
+    ap.add_argument("--stage", type=int, default=None, help="stage_neighbours with --launch (profiling runs)")
     return ap.parse_args()
 
 
@@ -187,7 +189,7 @@ def cpu_baseline(items, params, seconds: float, states=None, settle: int = 0):
             s.step(1)
         steps += 1
         el = time.perf_counter() - t0
-        if el >= seconds or steps >= 1000:
+        if el >= seconds or steps >= 100000:
             break
     for s in sims:
         s.close()
@@ -251,6 +253,8 @@ def main():
     sampler = ClockSampler(phys)
 
     params = scenes.physics_params(args.substeps)
+    if args.stage is not None:
+        params.stage_neighbours = args.stage
     items, nv, ne, nt = build_workload(args.garments, args.seed + rank)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
@@ -267,7 +271,11 @@ def main():
     pins = np.concatenate(pins).astype(np.uint32)
     pin_xyz0 = np.concatenate([c.xyz[c.pinned] for c, _ in items]).astype(np.float32)
     b.step(args.settle)  # drape the sheets over their spheres (untimed)
-    blk, ctas = (256, 0) if args.no_autotune else b.autotune()
+    if args.launch:
+        b.set_launch(*(int(v) for v in args.launch.split(",")))
+    elif not args.no_autotune:
+        b.autotune()
+    launch = b.launch_info()
 
     sampler.start()
     # ---- device-resident value: K steps replayed from CUDA graphs --------------------
@@ -360,7 +368,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": workload_name(args), "garments": args.garments, "vertices_per_gpu": nv,
                        "spring_entries": ne, "triangles": nt, "contacts": contacts,
-                       "launch": {"block": blk, "ctas_per_sm": ctas},
+                       "launch": launch,
                        "l2": f"inputs larger than L2: {alg_bytes / 1e6:.0f} MB moved per step vs 129 MB L2",
                        "parallelism": f"{world} independent batches (one per GPU)"},
             "e2e": {"value": e2e_value, "unit": "vertex-steps/s", "h2d_bytes_per_step": h2d,
@@ -373,7 +381,7 @@ def main():
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * launch["kernels_per_step"],
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

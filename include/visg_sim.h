@@ -252,6 +252,11 @@ int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm);
  * 0 for one CTA per tile.  For reproducible timings and for callers that tune
  * offline.  No counterpart in the reference (it launches one fixed shape). */
 int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas_per_sm);
+/* The launch shape and variant in use (any pointer may be NULL): block, ctas_per_sm
+ * (0 = one CTA per tile), split_collision and stage_neighbours as chosen (by the
+ * parameters or visg_batch_autotune), and the kernels one step launches. */
+int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm, int32_t* split_collision,
+                           int32_t* stage_neighbours, int32_t* kernels_per_step);
 int visg_batch_info(VisgBatch* b, int32_t* n_garments, int64_t* n_vertices,
                     int64_t* n_entries, int64_t* n_tris);
 int visg_batch_count_contacts(VisgBatch* b, int64_t* n);

@@ -85,6 +85,7 @@ def lib():
         "visg_batch_update_body": (C.c_int, [_vp, C.c_int32, _fp, _fp]),
         "visg_batch_autotune": (C.c_int, [_vp, _i32p, _i32p]),
         "visg_batch_set_launch": (C.c_int, [_vp, C.c_int32, C.c_int32]),
+        "visg_batch_launch_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, _i32p]),
         "visg_batch_read_positions_async": (C.c_int, [_vp, _vp]),
         "visg_batch_get_state": (C.c_int, [_vp, C.c_int32, _fp, _fp, _fp]),
         "visg_batch_set_state": (C.c_int, [_vp, C.c_int32, _fp, _fp, _fp]),
@@ -364,6 +365,12 @@ class BatchSimulator:
 
     def set_state(self, garment: int = -1, x=None, xo=None, n=None):
         _check(lib().visg_batch_set_state(self.h, garment, _p(_f32(x)), _p(_f32(xo)), _p(_f32(n))))
+
+    def launch_info(self) -> dict:
+        v = [C.c_int32() for _ in range(5)]
+        _check(lib().visg_batch_launch_info(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("block", "ctas_per_sm", "split_collision", "stage_neighbours", "kernels_per_step"),
+                        (x.value for x in v)))
 
     def set_launch(self, block: int, ctas_per_sm: int):
         _check(lib().visg_batch_set_launch(self.h, block, ctas_per_sm))

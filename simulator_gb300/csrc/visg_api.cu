@@ -1328,6 +1328,19 @@ int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas) {
     return b->eng.set_launch(block, ctas);
 }
 
+int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas, int32_t* split, int32_t* stage,
+                           int32_t* kernels) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    const Engine& e = b->eng;
+    const int v = e.variant(e.block);
+    if (block) *block = e.block;
+    if (ctas) *ctas = e.sm_count > 0 ? e.grid / e.sm_count : 0;
+    if (split) *split = (v & SV_SPLIT) ? 1 : 0;
+    if (stage) *stage = (v & SV_STAGED) ? 1 : 0;
+    if (kernels) *kernels = (v & SV_SPLIT) ? 2 : 1;
+    return VISG_OK;
+}
+
 int visg_batch_info(VisgBatch* b, int32_t* ng, int64_t* nv, int64_t* ne, int64_t* nt) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     Engine& e = b->eng;
