@@ -370,8 +370,12 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-__device__ __forceinline__ void mbar_init(uint32_t bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // one arrival that also announces `bytes` of transactions, then the copy that completes them
@@ -402,22 +406,29 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return true;
 }
 
-// thread 0: stage the sliced-ELL block of `tile` (if it has one) at shared address dst
-__device__ __forceinline__ void stage_entries(const StepArgs& a, int tile, uint32_t dst, uint32_t bar) {
+// thread 0: stage the sliced-ELL block of `tile` at shared address dst, completing
+// the buffer's `full` phase when it lands; a tile without a staged block completes
+// the phase at once (every tile takes one phase, so no warp runs ahead of the ring)
+__device__ __forceinline__ void stage_entries(const StepArgs& a, int tile, uint32_t dst, uint32_t full) {
     const int2 tw = __ldg(&a.twin[tile]);
     if (tw.y > 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the buffer come first
-        bulk_stage(dst, a.sell + (uint32_t)tw.x, (uint32_t)tw.y * 8u, bar);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the readers' loads come first
+        bulk_stage(dst, a.sell + (uint32_t)tw.x, (uint32_t)tw.y * 8u, full);
+    } else {
+        mbar_arrive(full);
     }
 }
 
 // The fused step: persistent CTAs walk the tile table.  With STAGED, thread 0 copies
 // the next tile's block of sliced-ELL entries (the tile's slices are contiguous: one
-// TMA bulk copy) into the other shared-memory buffer while the CTA computes the
+// TMA bulk copy) into the other shared-memory buffer while the warps compute the
 // current tile, so each spring's chain starts with a shared-memory load; tiles whose
-// block exceeds the buffer read their entries from global memory.  Waits are bounded:
-// a copy that has not landed after kWaitNs sets ERR_TIMEOUT, and the CTA waits (again
-// bounded) for its copies in flight and exits.
+// block exceeds the buffer read their entries from global memory.  No CTA barrier
+// per tile: warps report a finished buffer on its `empty` mbarrier and only thread 0
+// waits for it before refilling.  Waits are bounded: one that gives up after kWaitNs
+// sets ERR_TIMEOUT, the issuing thread waits (again bounded) for its copies in
+// flight, and the warp exits; warps left waiting on a copy that is never issued give
+// up the same way.
 template <int BLOCK, bool COLL, bool KD0, bool SPLIT, bool STAGED>
 __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
     extern __shared__ __align__(128) unsigned char dyn_smem[];
@@ -429,44 +440,52 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
             vertex_step<COLL, KD0, SPLIT, false>(a, __ldg(&a.tiles[tile]), a.sell, 0u, refv, check, perk, wild,
                                                  my_disp, my_bad);
     } else {
-        const uint32_t bar = smem_addr(dyn_smem);
-        const uint32_t buf0 = bar + kBarBytes;
+        // two-buffer ring: full[b] completes when buffer b holds its tile's block,
+        // empty[b] when every warp is done reading it
+        const uint32_t full = smem_addr(dyn_smem), empty = full + 16u;
+        const uint32_t buf0 = full + kBarBytes;
         const uint2* sbuf = reinterpret_cast<const uint2*>(dyn_smem + kBarBytes);
         const uint32_t bbytes = (uint32_t)a.win_cap * 8u;
+        const int lane = (int)(threadIdx.x & 31u);
         if (threadIdx.x == 0) {
-            mbar_init(bar);
-            mbar_init(bar + 8);
+            mbar_init(full, 1u);
+            mbar_init(full + 8u, 1u);
+            mbar_init(empty, BLOCK / 32);
+            mbar_init(empty + 8u, BLOCK / 32);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
         __syncthreads();
-        if (threadIdx.x == 0 && (int)blockIdx.x < a.n_tiles) stage_entries(a, blockIdx.x, buf0, bar);
-        uint32_t par = 0;  // parity of the next phase of each buffer's barrier
-        int b = 0;
-        for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, b ^= 1) {
+        if (threadIdx.x == 0 && (int)blockIdx.x < a.n_tiles) stage_entries(a, blockIdx.x, buf0, full);
+        int it = 0;
+        for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
+            const int b = it & 1;
+            const uint32_t par = (uint32_t)(it >> 1) & 1u;  // phase parity of this iteration's buffer
             const int nxt = tile + (int)gridDim.x;
-            if (threadIdx.x == 0 && nxt < a.n_tiles)
-                stage_entries(a, nxt, buf0 + (uint32_t)(b ^ 1) * bbytes, bar + 8u * (b ^ 1));
-            const int4 td = __ldg(&a.tiles[tile]);
-            const int2 tw = __ldg(&a.twin[tile]);
-            bool ok = true;
-            if (tw.y > 0) {
-                ok = __all_sync(0xffffffffu, mbar_wait(bar + 8u * b, (par >> b) & 1u));
-                par ^= 1u << b;
-                if (ok)
-                    vertex_step<COLL, KD0, SPLIT, true>(a, td, sbuf + (size_t)b * a.win_cap, (uint32_t)tw.x, refv,
-                                                        check, perk, wild, my_disp, my_bad);
-            } else {
-                vertex_step<COLL, KD0, SPLIT, false>(a, td, a.sell, 0u, refv, check, perk, wild, my_disp, my_bad);
+            bool pok = true;
+            if (threadIdx.x == 0 && nxt < a.n_tiles) {
+                // the other buffer was read in iteration it - 1: wait for every warp to finish it
+                if (it >= 1) pok = mbar_wait(empty + 8u * (b ^ 1), (uint32_t)((it - 1) >> 1) & 1u);
+                if (pok) stage_entries(a, nxt, buf0 + (uint32_t)(b ^ 1) * bbytes, full + 8u * (b ^ 1));
             }
-            if (__syncthreads_or(!ok)) {
-                // a copy did not land: record it, let this CTA's copies in flight finish, leave
+            const bool landed = mbar_wait(full + 8u * b, par);
+            if (!__all_sync(0xffffffffu, landed && pok)) {
+                // a wait gave up: record it; the issuing thread lets its copies in flight land
+                if (lane == 0) atomicOr(a.err, ERR_TIMEOUT);
                 if (threadIdx.x == 0) {
-                    atomicOr(a.err, ERR_TIMEOUT);
-                    if (tw.y > 0) mbar_wait(bar + 8u * b, ((par >> b) & 1u) ^ 1u);
-                    if (nxt < a.n_tiles && __ldg(&a.twin[nxt]).y > 0) mbar_wait(bar + 8u * (b ^ 1), (par >> (b ^ 1)) & 1u);
+                    mbar_wait(full + 8u * b, par);
+                    if (pok && nxt < a.n_tiles) mbar_wait(full + 8u * (b ^ 1), (uint32_t)((it + 1) >> 1) & 1u);
                 }
                 return;
             }
+            const int4 td = __ldg(&a.tiles[tile]);
+            const int2 tw = __ldg(&a.twin[tile]);
+            if (tw.y > 0)
+                vertex_step<COLL, KD0, SPLIT, true>(a, td, sbuf + (size_t)b * a.win_cap, (uint32_t)tw.x, refv, check,
+                                                    perk, wild, my_disp, my_bad);
+            else
+                vertex_step<COLL, KD0, SPLIT, false>(a, td, a.sell, 0u, refv, check, perk, wild, my_disp, my_bad);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + 8u * b);
         }
     }
     if (check) {
