@@ -78,7 +78,7 @@ int Engine::forward(int nsteps, int ckpt) {
     CU(launch_narrow(adj.s64 + 2 * (size_t)c * n3, d_stage, 2 * (int64_t)n3, stream));
     CU(launch_narrow(adj.s64 + 4 * n3, d_stage + 2 * n3, (int64_t)n3, stream));
     CU(launch_pack_state(d_state[cur], d_state[cur ^ 1], d_normal, N, d_stage, d_stage + n3, d_stage + 2 * n3, p.dt,
-                         d_wild, stream));
+                         step_params().drec, step_params().dmax, d_wild, stream));
     if (int r = sync()) return r;
     adj.ready = true;
     return VISG_OK;

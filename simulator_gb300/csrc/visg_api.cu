@@ -481,6 +481,10 @@ struct Engine {
         sp.n_lists = p.n_lists;
         sp.max_disp = p.max_displacement;
         sp.margin = p.collision_margin ? 1 : 0;
+        uint32_t kdb;
+        std::memcpy(&kdb, &p.spring_damping, 4);
+        sp.drec = (kdb == 0u && p.verlet_damping != 1.0f && p.n_lists >= 1) ? 1 : 0;
+        sp.dmax = 0.5e15f * p.dt;
         return sp;
     }
 
@@ -798,7 +802,8 @@ struct Engine {
         if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
         if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
         CU(launch_pack_state(d_state[cur] + 2 * v0, d_state[cur ^ 1] + 2 * v0, d_normal + v0, n, x ? sx : nullptr,
-                             xo ? sxo : nullptr, nrm ? sn : nullptr, p.dt, d_wild, stream));
+                             xo ? sxo : nullptr, nrm ? sn : nullptr, p.dt, step_params().drec,
+                             step_params().dmax, d_wild, stream));
         CU(cudaStreamSynchronize(stream));
         return VISG_OK;
     }

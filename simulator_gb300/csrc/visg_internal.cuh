@@ -4,6 +4,8 @@
 //   cloth state, double-buffered: 2 float4 per vertex
 //        [x.x x.y x.z v.x] [v.y v.z flags 0]             32 B, one sector per gather
 //        v = (x - x_old) / dt, computed once per step by the vertex's own thread;
+//        with StepParams::drec the record carries D = x - x_old in its place (then
+//        no spring reads a neighbour's velocity and the step needs only x - x_old);
 //        x_old is x (flag XO_IS_X) or the x of the same vertex in the other buffer;
 //        the last word is the query cache's margin: while the vertex stays within
 //        that distance of where its last first-hit query was answered, the answer
@@ -127,6 +129,8 @@ struct StepParams {
     int n_lists;
     float max_disp;
     int margin;  // keep each vertex's proven distance to its body's leaf boxes (collision margin)
+    int drec;    // records carry D = x - x_old instead of v (spring damping +0, Verlet damping != 1)
+    float dmax;  // tame bound on |D| (|v| = |D| / dt < 1e15)
 };
 
 struct StepArgs {
@@ -178,7 +182,8 @@ cudaError_t launch_unpack_state(const float4* state, const float4* other, const 
                                 float* xo, float* nrm, cudaStream_t s);
 // x/xo/nrm may be NULL (kept); dt recomputes v = (x - x_old) / dt
 cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x,
-                              const float* xo, const float* nrm, float dt, uint32_t* wild, cudaStream_t s);
+                              const float* xo, const float* nrm, float dt, int drec, float dmax, uint32_t* wild,
+                              cudaStream_t s);
 
 // forget the collision margin of vertices [v0, v1) (their body moved)
 cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s);

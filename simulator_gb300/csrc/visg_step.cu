@@ -139,14 +139,17 @@ __device__ __forceinline__ int query_leaf(const BvhView& bv, int n_leaves, int r
 // t0/t1 is the neighbour's record: position and velocity (p2 - p2_old) / dt, stored
 // once per step by the neighbour's own thread with the same IEEE division; nk = -k.
 // FAST drops the damping term, for spring damping exactly +0: see row_forces.
+// With drec the neighbour's record holds D = p2 - p2_old; its velocity is D / dt.
 template <bool FAST>
 __device__ __forceinline__ f3 spring_force(f3 x, f3 vel, float4 t0, float4 t1, float nk, float rest, float kd,
-                                           f3 eps3) {
+                                           f3 eps3, bool drec, float dt) {
     const f3 dP = add(sub(x, mk3(t0.x, t0.y, t0.z)), eps3);
     const float dist = __fsqrt_rn(dot(dP, dP));
     float c = __fmul_rn(nk, __fsub_rn(dist, rest));
     if (!FAST) {
-        const f3 dV = sub(vel, mk3(t0.w, t1.x, t1.y));
+        f3 v2 = mk3(t0.w, t1.x, t1.y);
+        if (drec) v2 = divs(v2, dt);
+        const f3 dV = sub(vel, v2);
         c = __fadd_rn(c, __fmul_rn(kd, __fdiv_rn(dot(dV, dP), dist)));
     }
     return mul(c, mul(dP, __frcp_rn(dist)));  // normalize(dP) = dP * (1 / |dP|)
@@ -173,7 +176,7 @@ struct Entries {
 template <bool FAST, class Rec, class Ent>
 __device__ __forceinline__ f3 list_sum(const Rec& rec, const Ent& ep, const float* __restrict__ kp, int e,
                                        const int end, const float nk, const bool perk, f3 x, f3 vel, float kd,
-                                       f3 eps3) {
+                                       f3 eps3, bool drec, float dt) {
     f3 acc = mk3(0.0f, 0.0f, 0.0f);
     for (; e + 1 < end; e += 2) {
         const uint2 ea = ep[e], eb = ep[e + 1];
@@ -182,8 +185,8 @@ __device__ __forceinline__ f3 list_sum(const Rec& rec, const Ent& ep, const floa
         const float4 a1 = FAST ? a0 : rec.r1(ja), b1 = FAST ? b0 : rec.r1(jb);
         const float ka = perk ? -__ldg(kp + 32 * e) : nk;
         const float kb = perk ? -__ldg(kp + 32 * (e + 1)) : nk;
-        const f3 fa = spring_force<FAST>(x, vel, a0, a1, ka, __uint_as_float(ea.y), kd, eps3);
-        const f3 fb = spring_force<FAST>(x, vel, b0, b1, kb, __uint_as_float(eb.y), kd, eps3);
+        const f3 fa = spring_force<FAST>(x, vel, a0, a1, ka, __uint_as_float(ea.y), kd, eps3, drec, dt);
+        const f3 fb = spring_force<FAST>(x, vel, b0, b1, kb, __uint_as_float(eb.y), kd, eps3, drec, dt);
         acc = add(add(acc, fa), fb);
     }
     if (e < end) {
@@ -192,7 +195,7 @@ __device__ __forceinline__ f3 list_sum(const Rec& rec, const Ent& ep, const floa
         const float4 a0 = rec.r0(ja);
         const float4 a1 = FAST ? a0 : rec.r1(ja);
         const float ka = perk ? -__ldg(kp + 32 * e) : nk;
-        acc = add(acc, spring_force<FAST>(x, vel, a0, a1, ka, __uint_as_float(ea.y), kd, eps3));
+        acc = add(acc, spring_force<FAST>(x, vel, a0, a1, ka, __uint_as_float(ea.y), kd, eps3, drec, dt));
     }
     return acc;
 }
@@ -207,7 +210,8 @@ __device__ __forceinline__ f3 row_forces(const Rec& rec, const Ent& ep, const fl
     for (int l = 0; l < VISG_MAX_LISTS; ++l) {
         if (l < P.n_lists) {
             const int n = (int)(((l < 2 ? cnt.x : cnt.y) >> (16 * (l & 1))) & (l == 3 ? 0x7fffu : 0xffffu));
-            F = add(F, list_sum<FAST>(rec, ep, kp, e, e + n, -P.list_k[l], perk, x, vel, P.kd, eps3));
+            F = add(F, list_sum<FAST>(rec, ep, kp, e, e + n, -P.list_k[l], perk, x, vel, P.kd, eps3, P.drec != 0,
+                                      P.dt));
             e += n;
         }
     }
@@ -220,6 +224,12 @@ __device__ __forceinline__ f3 row_forces(const Rec& rec, const Ent& ep, const fl
 __device__ __forceinline__ bool tame(f3 x, f3 v) {
     const float m = 1e15f;
     return fabsf(x.x) < m && fabsf(x.y) < m && fabsf(x.z) < m && fabsf(v.x) < m && fabsf(v.y) < m && fabsf(v.z) < m;
+}
+// the same for a record that carries D = x - x_old (dmax = 0.5e15 dt, so |D / dt| < 1e15)
+__device__ __forceinline__ bool tame_d(f3 x, f3 d, float dmax) {
+    const float m = 1e15f;
+    return fabsf(x.x) < m && fabsf(x.y) < m && fabsf(x.z) < m && fabsf(d.x) < dmax && fabsf(d.y) < dmax &&
+           fabsf(d.z) < dmax;
 }
 
 // One thread's vertex of tile td = {garment, first vertex, end vertex, first slice}.
@@ -241,7 +251,7 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
     const float4 s0 = rec.r0(ii);
     const float4 s1 = rec.r1(ii);
     const f3 x = mk3(s0.x, s0.y, s0.z);
-    const f3 vel = mk3(s0.w, s1.x, s1.y);
+    const f3 rv = mk3(s0.w, s1.x, s1.y);  // v, or D = x - x_old with drec
     const uint32_t flags = __float_as_uint(s1.z);
     const uint2 cnt = __ldg(&a.vcount[ii]);
     const bool pinned = (cnt.y & PIN_BIT) != 0u;
@@ -250,10 +260,22 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
     if (active && !pinned) {
         const int lane = (int)(threadIdx.x & 31u);
         const uint32_t sb = __ldg(&a.slice_off[td.w + (int)(threadIdx.x >> 5)]) + (uint32_t)lane;  // row entry 0
-        const f3 xo = (flags & FLAG_XO_IS_X) ? x : xyz(a.state_out[2 * ii]);
+        // x - x_old: from the record (drec), else from x_old in the other buffer
+        f3 xo = x, d = rv, vel = rv;
+        if (!P.drec) {
+            if (!(flags & FLAG_XO_IS_X)) xo = xyz(a.state_out[2 * ii]);
+            d = sub(x, xo);
+        }
         f3 np = mk3(0.0f, 0.0f, 0.0f);
         if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
-        const f3 F0 = add(mul(grav, P.mass), mul(vel, P.damp));
+        // force damping: with drec and damping exactly +0 the term v * +0 is a signed
+        // zero for every tame v, and g m + (+-0) only differs in the sign of a zero
+        // component, which the first list's sum (never -0) erases
+        f3 F0 = mul(grav, P.mass);
+        if (!P.drec || __float_as_uint(P.damp) != 0u || wild) {
+            if (P.drec) vel = divs(rv, P.dt);
+            F0 = add(F0, mul(vel, P.damp));
+        }
         const Entries<SMEM_ENT> ep{ebase + (sb - e0)};
         const float* kp = perk ? a.sellk + sb : nullptr;
         f3 F;
@@ -265,15 +287,17 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
             // the wild flag says when one was not) or c is not finite (then F is not
             // finite either: such rows are recomputed with the damping term).
             F = row_forces<true>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
-            if (wild || !(isfinite(F.x) && isfinite(F.y) && isfinite(F.z)))
+            if (wild || !(isfinite(F.x) && isfinite(F.y) && isfinite(F.z))) {
+                if (P.drec) vel = divs(rv, P.dt);
                 F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
+            }
         } else {
             F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
         }
         F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
         const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
-        if (refv) xn = add(sub(add(x, x), xo), adt);
-        else xn = add(add(x, mul(P.gamma, sub(x, xo))), adt);
+        if (refv) xn = add(sub(add(x, x), xo), adt);  // never with drec
+        else xn = add(add(x, mul(P.gamma, d)), adt);
         xon = x;
     }
     // Query cache.  s1.w holds a margin: while the vertex stays within that L-infinity
@@ -338,8 +362,9 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
     bool untamed = false;
     if (active) {
         const bool xo_is_x = pinned || has_n;
-        const f3 vn = divs(sub(xn, xon), P.dt);
-        untamed = !tame(xn, vn);
+        const f3 dn = sub(xn, xon);
+        const f3 vn = P.drec ? dn : divs(dn, P.dt);  // what the record carries
+        untamed = P.drec ? !tame_d(xn, dn, P.dmax) : !tame(xn, vn);
         const uint32_t fl = (has_n ? FLAG_HAS_NORMAL : 0u) | (xo_is_x ? FLAG_XO_IS_X : 0u) |
                             (cached && skin > 0.0f ? FLAG_LEAF_CACHED : 0u);
         a.state_out[2 * i] = make_float4(xn.x, xn.y, xn.z, vn.x);
@@ -348,8 +373,9 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
         if (check) {
             const float dd = fmaxf(fabsf(__fsub_rn(xn.x, x.x)),
                                    fmaxf(fabsf(__fsub_rn(xn.y, x.y)), fabsf(__fsub_rn(xn.z, x.z))));
-            if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(vn.x) || !isfinite(vn.y) ||
-                !isfinite(vn.z))
+            const f3 vc = P.drec ? divs(dn, P.dt) : vn;
+            if (!isfinite(xn.x) || !isfinite(xn.y) || !isfinite(xn.z) || !isfinite(vc.x) || !isfinite(vc.y) ||
+                !isfinite(vc.z))
                 ++my_bad;
             else
                 my_disp = fmaxf(my_disp, dd);
@@ -694,7 +720,7 @@ __global__ void k_unpack_state(const float4* __restrict__ st, const float4* __re
 // x == nullptr keeps x, etc.  x_old is written into the other buffer and v is
 // recomputed as (x - x_old) / dt; a vertex has a stored normal iff it is non-zero.
 __global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, const float* x, const float* xo,
-                             const float* nrm, float dt, uint32_t* wild) {
+                             const float* nrm, float dt, int drec, float dmax, uint32_t* wild) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 s0 = st[2 * i], s1 = st[2 * i + 1];
@@ -703,7 +729,7 @@ __global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, c
     const f3 xo0 = (fl & FLAG_XO_IS_X) ? x0 : xyz(other[2 * i]);
     const f3 xv = x ? mk3(x[3 * i], x[3 * i + 1], x[3 * i + 2]) : x0;
     const f3 xov = xo ? mk3(xo[3 * i], xo[3 * i + 1], xo[3 * i + 2]) : xo0;
-    const f3 v = divs(sub(xv, xov), dt);
+    const f3 v = drec ? sub(xv, xov) : divs(sub(xv, xov), dt);  // what the record carries
     if (nrm) {
         const float a = nrm[3 * i], b = nrm[3 * i + 1], c = nrm[3 * i + 2];
         const bool h = a != 0.0f || b != 0.0f || c != 0.0f;
@@ -714,7 +740,7 @@ __global__ void k_pack_state(float4* st, float4* other, float4* nr, int64_t n, c
     other[2 * i] = make_float4(xov.x, xov.y, xov.z, 0.0f);
     st[2 * i] = make_float4(xv.x, xv.y, xv.z, v.x);
     st[2 * i + 1] = make_float4(v.y, v.z, __uint_as_float(fl), 0.0f);
-    if (!tame(xv, v)) atomicOr(wild, 1u);
+    if (drec ? !tame_d(xv, v, dmax) : !tame(xv, v)) atomicOr(wild, 1u);
 }
 
 __global__ void k_check_tame(const float4* __restrict__ st, int64_t n, uint32_t* wild) {
@@ -825,9 +851,9 @@ cudaError_t launch_set_vertices(float4* state, const uint32_t* idx, const float*
 }
 
 cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int64_t n, const float* x, const float* xo,
-                              const float* nrm, float dt, uint32_t* wild, cudaStream_t s) {
+                              const float* nrm, float dt, int drec, float dmax, uint32_t* wild, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm, dt, wild);
+    k_pack_state<<<grid_for(n, 256), 256, 0, s>>>(state, other, normal, n, x, xo, nrm, dt, drec, dmax, wild);
     return cudaGetLastError();
 }
 

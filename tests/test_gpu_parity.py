@@ -320,8 +320,14 @@ def test_staged_and_unstaged_tiles_mixed_vs_oracle():
         assert np.array_equal(u, v)
 
 
-def test_set_vertex_and_state_roundtrip():
+@pytest.mark.parametrize("physics", ["reference", "config"])
+def test_set_vertex_and_state_roundtrip(physics):
+    # reference physics: records carry v; config physics (spring damping 0, damped
+    # Verlet): records carry x - x_old
     cloth, cl, body, p = ref_scene(side=16, subdiv=2)
+    if physics == "config":
+        p = config_params(substeps=2)
+        cl = cloth.lists
     g = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
     o = OracleSim(p, cloth.xyz, cl, body.xyz, body.tris, body.normals, prec=4)
     g.simulate(40)
