@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-garment loop")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-moving", action="store_true", help="skip the moving-body plain configs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--launch", default=None, help="block,ctas_per_sm instead of autotuning (profiling runs)")
@@ -196,6 +197,53 @@ def cpu_baseline(items, params, seconds: float, states=None, settle: int = 0):
     return {"value": nv * steps / el, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
             "sample": f"the first {len(items)} garments ({nv} vertices) from the draped state, {steps} steps "
                       f"({el:.1f} s), {threads} OpenMP threads"}
+
+
+def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: int):
+    """The plain single-garment workloads whose body moves (LBVH rebuilt every step):
+    per step the body's positions (precomputed on the device) go in through
+    update_body_device, then one step runs.  Also times the same steps with the
+    body held still, so the rebuild's share shows."""
+    out = {}
+    for name, make in (("garment_over_capsules", scenes.garment_over_capsules),
+                       ("sheet_over_noisy_sphere", scenes.sheet_over_noisy_sphere)):
+        cloth, body, motion = make(0)
+        n = len(cloth.xyz)
+        sim = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
+                           pinned=cloth.pinned)
+        sim.set_stream(stream.cuda_stream)
+        total = warmup + 2 * steps
+        base = body.xyz.astype(np.float64)
+        frames = np.stack([(base + motion(k * params.dt)).astype(np.float32) for k in range(total)])
+        d_frames = torch.from_numpy(frames).cuda()
+        d_nrm = torch.from_numpy(np.ascontiguousarray(body.normals, np.float32)).cuda()
+        fb = d_frames.element_size() * base.size
+
+        def run(k0, k, move):
+            for j in range(k0, k0 + k):
+                if move:
+                    sim.update_body_device(d_frames.data_ptr() + j * fb, d_nrm.data_ptr())
+                sim.simulate(1)
+
+        run(0, warmup, True)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        run(warmup, steps, True)
+        e[1].record(stream)
+        e[2].record(stream)
+        run(warmup + steps, steps, False)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        ms_move = e[0].elapsed_time(e[1]) / steps
+        ms_still = e[2].elapsed_time(e[3]) / steps
+        out[name] = {"vertices": n, "spring_entries": int(sum(sl.n_entries for sl in cloth.lists)),
+                     "triangles": int(len(body.tris)), "steps": steps,
+                     "value": n / (ms_move / 1e3), "unit": "vertex-steps/s", "ms_per_step": ms_move,
+                     "ms_per_step_body_still": ms_still, "lbvh_rebuild_ms": ms_move - ms_still,
+                     "contacts": sim.count_contacts()}
+        sim.close()
+    return out
 
 
 # ---------------------------------------------------------------------------------------
@@ -344,6 +392,9 @@ def main():
                  "how": "each garment its own Simulator, stepped K steps (graph replay) one garment after another"}
         for s in sims:
             s.close()
+    moving = None
+    if rank == 0 and not args.no_moving:
+        moving = moving_body_configs(vs, scenes, torch, params, stream, 100, 10)
     clocks = sampler.stop()
 
     # ---- roofline of the fused step kernel ---------------------------------------------
@@ -380,6 +431,7 @@ def main():
                          "kernel": "k_step (fused integrate + springs + collision)",
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
+            "moving_body_configs": moving,
             "clocks": clocks,
             "gpu_launches": args.steps * launch["kernels_per_step"],
         }

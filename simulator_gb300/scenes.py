@@ -255,6 +255,26 @@ def physics_params(substeps: int = 2, **overrides):
                        ph["verlet_damping"], ph["thickness"], ph["box_depth"], ph["list_k"])
 
 
+def garment_over_capsules(seed: int = 0):
+    """The garment-scale plain workload: a 112 x 112 sheet (1 m) with positions
+    jittered by N(0, 1e-4 m), two corners pinned, over a torso and two arms
+    (19,392 triangles) that translate along -y at 0.5 m/s (the LBVH is rebuilt every
+    step).  Returns (cloth, body, motion) with motion(t) the body offset at time t."""
+    cloth = grid_cloth(112, 1.0, 0.0, jitter=1e-4, seed=seed)
+    body = three_capsules()
+    return cloth, body, lambda t: np.array([0.0, -0.5 * t, 0.0])
+
+
+def sheet_over_noisy_sphere(seed: int = 0):
+    """The large plain workload: a 512 x 512 sheet (1 m), two corners pinned, over an
+    icosphere of subdivision 7 (327,680 triangles, radius 0.3 m, vertices radially
+    perturbed by U(+-2%)) centred 0.5 m below, oscillating along y on a 1 Hz sine of
+    amplitude 0.1 m (the LBVH is rebuilt every step)."""
+    cloth = grid_cloth(512, 1.0, 0.0)
+    body = icosphere(7, 0.3, center=(0.0, -0.5, 0.0), noise=0.02, seed=seed)
+    return cloth, body, lambda t: np.array([0.0, 0.1 * np.sin(2.0 * np.pi * t), 0.0])
+
+
 def sheet_over_sphere(side: int = 64, subdiv: int = 4, radius: float = 0.3, seed: int = 0):
     """64x64 sheet (1 m) with two pinned corners above an icosphere 0.5 m below."""
     cloth = grid_cloth(side, 1.0, 0.0)
