@@ -16,7 +16,8 @@
 //   k_unique      keep the first triangle of every distinct code
 //                 (remove_redundant, Utilities.h:35-55), look-back compaction
 //   k_build       bottom-up radix-tree build fused with the refit: each leaf thread
-//                 climbs, the parent of range [l, r] is the boundary with the longer
+//                 climbs (handshakes in shared memory while both children lie in the
+//                 CTA's chunk of leaves, in global memory above), the parent of range [l, r] is the boundary with the longer
 //                 common prefix (delta(l-1,l) vs delta(r,r+1), delta = clz(a ^ b) as
 //                 cudaBRT.cu:9-19), the second child to arrive merges both boxes into
 //                 the identity box (calculateBoudingBox, cudaBRT.cu:166-206) and
@@ -375,50 +376,152 @@ __device__ __forceinline__ int delta_at(const uint32_t* c, int i, int j, int n) 
     return (j < 0 || j >= n) ? -1 : __clz((int)(c[i] ^ c[j]));
 }
 
-__global__ void __launch_bounds__(BUILD_THREADS)
+// release/acquire add on a global counter (orders this thread's node writes before
+// the add, and the sibling's writes before this thread's later reads)
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// identity box (min +100, max -100) expanded by child A then child B
+__device__ __forceinline__ void merge_ab(float4 alo, float4 ahi, float4 blo, float4 bhi, float4& lo, float4& hi) {
+    lo = make_float4(fminf(fminf(100.0f, alo.x), blo.x), fminf(fminf(100.0f, alo.y), blo.y),
+                     fminf(fminf(100.0f, alo.z), blo.z), 0.0f);
+    hi = make_float4(fmaxf(fmaxf(-100.0f, ahi.x), bhi.x), fmaxf(fmaxf(-100.0f, ahi.y), bhi.y),
+                     fmaxf(fmaxf(-100.0f, ahi.z), bhi.z), 0.0f);
+}
+
+// Bottom-up build in two phases.  Each CTA owns the BUILD_LEAVES sorted leaves
+// [c0, c1).  Phase 1 climbs through the nodes split inside the chunk
+// (c0 <= g <= c1 - 2) with the handshake in shared memory: each child leaves its
+// box, link and far range end in its side of the node's slot; the first to arrive
+// stops, the second merges and climbs on.  A node whose other child lies in another
+// chunk never sees a second local arrival.  After one CTA barrier, phase 2 resumes
+// each such climb (and every climb that reached a node split outside the chunk)
+// with the handshake in global memory through acquire/release atomics.  Every node
+// still gets both child boxes (and its leaf range) written into global memory, in
+// the same A-then-B merge order, so the tree and the boxes are those of a single
+// global climb.
+constexpr int BUILD_LEAVES = 512;
+__global__ void __launch_bounds__(BUILD_LEAVES)
 k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, const float4* __restrict__ tri_box,
         const float4* __restrict__ tri_leaf, Node* nodes, float4* __restrict__ leaves, uint32_t* flags, int2* range,
         BvhRoot* root, int* err) {
+    __shared__ uint32_t s_flag[BUILD_LEAVES];
+    // per node and side (A, B): lo (w = link), hi (w = far range end)
+    __shared__ float4 s_lo[BUILD_LEAVES][2], s_hi[BUILD_LEAVES][2];
     const int nt = root->n_tris;
     const int n = min(root->n_leaves, nt);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t t = min(utri[i], (uint32_t)(nt - 1));
-    leaves[2 * i] = tri_leaf[2 * t];
-    leaves[2 * i + 1] = tri_leaf[2 * t + 1];
-    float4 lo = tri_box[2 * t], hi = tri_box[2 * t + 1];
-    if (n == 1) {
-        root->root = -1;
-        root->top_lo = lo;
-        root->top_hi = hi;
-        return;
+    const int c0 = blockIdx.x * BUILD_LEAVES;
+    const int c1 = min(c0 + BUILD_LEAVES, n);
+    s_flag[threadIdx.x] = 0u;
+    __syncthreads();
+    const int i = c0 + (int)threadIdx.x;
+    int l = i, r = i, link = ~i;  // the current subtree: leaf range, link
+    float4 lo = make_float4(0.0f, 0.0f, 0.0f, 0.0f), hi = lo;
+    bool live = i < n;  // still climbing
+    int pend = -1;      // node where phase 1 stopped as the first local arrival
+    if (live) {
+        const uint32_t t = min(utri[i], (uint32_t)(nt - 1));
+        leaves[2 * i] = tri_leaf[2 * t];
+        leaves[2 * i + 1] = tri_leaf[2 * t + 1];
+        lo = tri_box[2 * t];
+        hi = tri_box[2 * t + 1];
+        if (n == 1) {
+            root->root = -1;
+            root->top_lo = lo;
+            root->top_hi = hi;
+            live = false;
+        }
     }
-    int l = i, r = i;
-    int link = ~i;
-    // a leaf climbs at most 31 levels (distinct 30-bit codes); the bound only guards
-    // against a corrupted input after a failed look-back
-    for (int level = 0;; ++level) {
-        if (level > 64) {
+    // phase 1: handshakes in shared memory for nodes split inside the chunk
+    int level = 0;
+    while (live) {
+        if (++level > 64) {  // a climb is at most 31 levels over distinct 30-bit codes
             atomicOr(err, ERR_TIMEOUT);
-            return;
+            live = false;
+            break;
         }
         const int dl = delta_at(ucode, l, l - 1, n);
         const int dr = delta_at(ucode, r, r + 1, n);
-        int g;
-        if (dr > dl) {  // the parent extends to the right: this node is child A, split r
-            g = r;
+        const bool is_a = dr > dl;  // the parent extends to the right: this node is child A
+        const int g = is_a ? r : l - 1;
+        if (g < c0 || g > c1 - 2) break;  // split outside the chunk: phase 2
+        if (is_a) {
             nodes[g].a_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
             nodes[g].a_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
-            range[g].x = l;
-        } else {  // child B of the parent split at l - 1
-            g = l - 1;
+            range[g].x = l;  // leaf ranges of the nodes (read by the export)
+        } else {
             nodes[g].b_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
             nodes[g].b_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
             range[g].y = r;
         }
-        __threadfence();
-        if (atomicAdd(&flags[g], 1u) == 0u) return;  // first child to arrive stops
-        __threadfence();
+        const int k = g - c0, side = is_a ? 0 : 1;
+        s_lo[k][side] = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+        s_hi[k][side] = make_float4(hi.x, hi.y, hi.z, __int_as_float(is_a ? l : r));
+        __threadfence_block();
+        if (atomicAdd(&s_flag[k], 1u) == 0u) {  // first to arrive: the sibling may be in another chunk
+            pend = g;
+            live = false;
+            break;
+        }
+        __threadfence_block();
+        // second to arrive: the sibling's side of the slot is complete
+        const float4 olo = s_lo[k][side ^ 1], ohi = s_hi[k][side ^ 1];
+        const int far = __float_as_int(ohi.w);
+        if (is_a) {
+            merge_ab(lo, hi, olo, ohi, lo, hi);
+            r = far;
+        } else {
+            merge_ab(olo, ohi, lo, hi, lo, hi);
+            l = far;
+        }
+        link = g;
+        if (l == 0 && r == n - 1) {
+            root->root = g;
+            root->top_lo = lo;
+            root->top_hi = hi;
+            live = false;
+            break;
+        }
+    }
+    __syncthreads();
+    // a climb that stopped first at a node whose other child never arrived locally
+    // resumes there: that child is in another chunk
+    bool resume = false;
+    if (pend >= 0 && s_flag[pend - c0] == 1u) {
+        live = true;
+        resume = true;
+        level = 0;
+    }
+    // phase 2: global handshakes.  A resumed climb re-enters at `pend` (its box and
+    // range are already in the node); the others continue from their current subtree.
+    while (live) {
+        if (++level > 64) {
+            atomicOr(err, ERR_TIMEOUT);
+            return;
+        }
+        int g;
+        if (resume) {
+            g = pend;
+            resume = false;
+        } else {
+            const int dl = delta_at(ucode, l, l - 1, n);
+            const int dr = delta_at(ucode, r, r + 1, n);
+            const bool is_a = dr > dl;
+            g = is_a ? r : l - 1;
+            if (is_a) {
+                nodes[g].a_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+                nodes[g].a_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
+                range[g].x = l;
+            } else {
+                nodes[g].b_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+                nodes[g].b_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
+                range[g].y = r;
+            }
+        }
+        if (atomic_add_acq_rel(&flags[g], 1u) == 0u) return;  // first child to arrive stops
         flags[g] = 0u;  // both children seen: ready for the next build
         const int2 rg = __ldcg(&range[g]);
         l = rg.x;
@@ -429,11 +532,7 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
         }
         const float4 alo = __ldcg(&nodes[g].a_lo), ahi = __ldcg(&nodes[g].a_hi);
         const float4 blo = __ldcg(&nodes[g].b_lo), bhi = __ldcg(&nodes[g].b_hi);
-        // identity box (min +100, max -100) expanded by child A then child B
-        lo = make_float4(fminf(fminf(100.0f, alo.x), blo.x), fminf(fminf(100.0f, alo.y), blo.y),
-                         fminf(fminf(100.0f, alo.z), blo.z), 0.0f);
-        hi = make_float4(fmaxf(fmaxf(-100.0f, ahi.x), bhi.x), fmaxf(fmaxf(-100.0f, ahi.y), bhi.y),
-                         fmaxf(fmaxf(-100.0f, ahi.z), bhi.z), 0.0f);
+        merge_ab(alo, ahi, blo, bhi, lo, hi);
         link = g;
         if (l == 0 && r == n - 1) {
             root->root = g;
@@ -503,7 +602,7 @@ cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_e
     }
     k_unique<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, b.nt, b.ucode, b.utri, ustat, ucount, b.tiles_sort,
                                                    b.root, d_err);
-    k_build<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes,
+    k_build<<<cdiv(b.nt, BUILD_LEAVES), BUILD_LEAVES, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes,
                                                                 b.leaves, b.flags, b.range, b.root, d_err);
     return cudaGetLastError();
 }
