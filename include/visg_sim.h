@@ -145,6 +145,22 @@ int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n);
  * synchronises and reports any device-side error (divergence, timeout). */
 int visg_get_positions(VisgSim* sim, float* out, int32_t on_device);
 
+/* The rest of cuda_update_vbo (simulation.cu:196-231), headless.  visg_set_faces gives
+ * the cloth's triangles (as the Simulator constructor takes them from the Mesh,
+ * simulation.cu:88-95); visg_render then writes, into caller buffers (device when
+ * on_device = 1, else host; any may be NULL): pos4 = n_vertices x (x, y, z, 1)
+ * (update_vbo_pos, verlet.cu:119-127), face_normals = n_faces x 3
+ * (compute_face_normal, verlet.cu:91-116: normalize(cross(p1 - p0, p2 - p0))) and
+ * vertex_normals = n_vertices x 3 (compute_vbo_normal, verlet.cu:163-181: the
+ * normalised sum of the vertex's face normals in face order; NaN for a vertex with
+ * no face, as there).  With normals_of_previous = 1 the normals are of the positions
+ * the last step started from, as the reference computes them; 0 uses the current
+ * positions (also the case before the first step and after visg_set_state).  Host
+ * outputs synchronise and report device-side errors. */
+int visg_set_faces(VisgSim* sim, const uint32_t* faces, int32_t n_faces);
+int visg_render(VisgSim* sim, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
+                int32_t normals_of_previous);
+
 /* Pipelined read-back (no counterpart in the reference, whose cuda_update_vbo
  * copies synchronously every frame): enqueues, behind the steps issued so far, the
  * copy of all n_vertices*3 positions into host memory `out` (page-locked memory
@@ -234,6 +250,11 @@ int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t 
 /* visg_get_state / visg_set_state of one garment (garment = -1: all, concatenated). */
 int visg_batch_get_state(VisgBatch* b, int32_t garment, float* x, float* x_old, float* normal);
 int visg_batch_set_state(VisgBatch* b, int32_t garment, const float* x, const float* x_old, const float* normal);
+/* visg_set_faces for one garment (local vertex indices); visg_render over all
+ * garments, concatenated in id order (face normals: garment 0's faces first). */
+int visg_batch_set_faces(VisgBatch* b, int32_t garment, const uint32_t* faces, int32_t n_faces);
+int visg_batch_render(VisgBatch* b, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
+                      int32_t normals_of_previous);
 /* visg_read_positions_async / visg_wait_positions over all garments (concatenated). */
 int visg_batch_read_positions_async(VisgBatch* b, float* out);
 int visg_batch_wait_positions(VisgBatch* b);

@@ -50,6 +50,7 @@ def lib():
         L.orc_sim_backward.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_springs_from_mesh.argtypes = [_fp, C.c_int, _u32p, C.c_int, _u32p, C.c_void_p, _i32p,
                                             _u32p, C.c_void_p, _i32p]
+        L.orc_render.argtypes = [_fp, _fp, C.c_int, _u32p, C.c_int, _fp, _fp, _fp]
         _lib = L
     return _lib
 
@@ -185,6 +186,20 @@ class OracleSim:
         return dk, ds
 
 
+def render(x, x_prev, faces):
+    """The reference's output stage (update_vbo_pos, compute_face_normal,
+    compute_vbo_normal) restated: (pos4, vertex normals, face normals)."""
+    x = np.ascontiguousarray(x, np.float32)
+    xp = np.ascontiguousarray(x_prev, np.float32)
+    f = np.ascontiguousarray(faces, np.uint32)
+    n, nf = len(x), len(f)
+    pos4 = np.zeros((n, 4), np.float32)
+    vn = np.zeros((n, 3), np.float32)
+    fn = np.zeros((nf, 3), np.float32)
+    lib().orc_render(ptr(x, _fp), ptr(xp, _fp), n, ptr(f, _u32p), nf, ptr(pos4, _fp), ptr(vn, _fp), ptr(fn, _fp))
+    return pos4, vn, fn
+
+
 def springs_from_mesh(xyz, tris):
     """Reference spring topology (create_neigh + CSR_spring) as two SpringLists."""
     from simulator_gb300.scenes import SPRING_DTYPE, SpringList
@@ -235,10 +250,27 @@ def hlib():
         L.ref_sim_n_leaves.argtypes = [C.c_void_p]
         L.ref_sim_export_lbvh.argtypes = [C.c_void_p, _u32p, _fp, _u32p, _i32p, _i32p, _i32p, _i32p, _i32p, _fp,
                                           _fp, _fp]
+        L.ref_render.argtypes = [_fp, _fp, C.c_int, _u32p, C.c_int, _fp, _fp, _fp]
         if L.ref_init(CUBIN_PATH.encode()) != 0:
             raise RuntimeError("refkern init failed: " + L.ref_last_error().decode())
         _hlib = L
     return _hlib
+
+
+def ref_render(x, x_prev, faces):
+    """The reference's own update_vbo_pos / compute_face_normal / compute_vbo_normal
+    kernels on the GPU: (pos4, vertex normals, face normals)."""
+    x = np.ascontiguousarray(x, np.float32)
+    xp = np.ascontiguousarray(x_prev, np.float32)
+    f = np.ascontiguousarray(faces, np.uint32)
+    n, nf = len(x), len(f)
+    pos4 = np.zeros((n, 4), np.float32)
+    vn = np.zeros((n, 3), np.float32)
+    fn = np.zeros((max(nf, 1), 3), np.float32)
+    if hlib().ref_render(ptr(x, _fp), ptr(xp, _fp), n, ptr(f, _u32p), nf, ptr(pos4, _fp), ptr(vn, _fp),
+                         ptr(fn, _fp)) != 0:
+        raise RuntimeError("ref_render: " + hlib().ref_last_error().decode())
+    return pos4, vn, fn[:nf]
 
 
 class RefSim:

@@ -46,6 +46,7 @@ static_assert(sizeof(RPrim) == 32, "Primitive layout");
 std::string g_msg;
 CUmodule g_mod = nullptr;
 CUfunction f_verlet, f_morton, f_init_nodes, f_internal, f_refit;
+CUfunction f_vbo_pos = nullptr, f_face_normal = nullptr, f_vbo_normal = nullptr;
 
 int fail(const std::string& m) {
     g_msg = m;
@@ -257,6 +258,57 @@ int ref_init(const char* cubin) {
         find_fn("_Z10init_nodes", &f_init_nodes) || find_fn("_Z19processInternalNode", &f_internal) ||
         find_fn("_Z19calculateBoudingBox", &f_refit))
         return -1;
+    return 0;
+}
+
+// The output stage of Simulator::cuda_update_vbo (simulation.cu:196-231) with the
+// reference's own kernels: update_vbo_pos on x (the positions after the step),
+// compute_face_normal on x_prev (the positions the step started from), then
+// compute_vbo_normal over the vertex -> face CSR that get_vertex_adjface
+// (simulation.cu:152-180) builds; device buffers stand in for the GL buffers.
+int ref_render(const float* x, const float* x_prev, int n, const uint32_t* faces, int nf, float* pos4, float* vn,
+               float* fn) {
+    if (!f_vbo_pos && (find_fn("_Z14update_vbo_pos", &f_vbo_pos) || find_fn("_Z19compute_face_normal", &f_face_normal) ||
+                       find_fn("_Z18compute_vbo_normal", &f_vbo_normal)))
+        return -1;
+    std::vector<std::vector<uint32_t>> adj(n);
+    for (int f = 0; f < nf; ++f)
+        for (int j = 0; j < 3; ++j) adj[faces[3 * f + j]].push_back((uint32_t)f);
+    std::vector<uint32_t> row, col;
+    uint32_t start = 0;
+    for (int i = 0; i < n; ++i) {
+        row.push_back(start);
+        start += (uint32_t)adj[i].size();
+        for (uint32_t f : adj[i]) col.push_back(f);
+    }
+    row.push_back(start);
+    float *dx, *dxp, *dpos, *dvn, *dfn;
+    uint32_t *dfaces, *drow, *dcol;
+    RT(cudaMalloc((void**)&dx, 12 * (size_t)n));
+    RT(cudaMalloc((void**)&dxp, 12 * (size_t)n));
+    RT(cudaMalloc((void**)&dpos, 16 * (size_t)n));
+    RT(cudaMalloc((void**)&dvn, 12 * (size_t)n));
+    RT(cudaMalloc((void**)&dfn, 12 * (size_t)nf + 12));
+    RT(cudaMalloc((void**)&dfaces, 12 * (size_t)nf + 12));
+    RT(cudaMalloc((void**)&drow, 4 * row.size()));
+    RT(cudaMalloc((void**)&dcol, 4 * col.size() + 4));
+    RT(cudaMemcpy(dx, x, 12 * (size_t)n, cudaMemcpyHostToDevice));
+    RT(cudaMemcpy(dxp, x_prev, 12 * (size_t)n, cudaMemcpyHostToDevice));
+    RT(cudaMemcpy(dfaces, faces, 12 * (size_t)nf, cudaMemcpyHostToDevice));
+    RT(cudaMemcpy(drow, row.data(), 4 * row.size(), cudaMemcpyHostToDevice));
+    if (!col.empty()) RT(cudaMemcpy(dcol, col.data(), 4 * col.size(), cudaMemcpyHostToDevice));
+    unsigned un = (unsigned)n, idx_size = 3u * (unsigned)nf;
+    void* a1[] = {&dpos, &dx, &un};
+    if (launch(f_vbo_pos, (un + 511) / 512, 512, a1)) return -1;
+    void* a2[] = {&dxp, &dfaces, &idx_size, &dfn};
+    if (nf > 0 && launch(f_face_normal, ((unsigned)nf + 511) / 512, 512, a2)) return -1;
+    void* a3[] = {&dvn, &drow, &dcol, &dfn, &un};
+    if (launch(f_vbo_normal, (un + 1023) / 1024, 1024, a3)) return -1;
+    RT(cudaMemcpy(pos4, dpos, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+    RT(cudaMemcpy(vn, dvn, 12 * (size_t)n, cudaMemcpyDeviceToHost));
+    if (nf > 0) RT(cudaMemcpy(fn, dfn, 12 * (size_t)nf, cudaMemcpyDeviceToHost));
+    void* ps[] = {dx, dxp, dpos, dvn, dfn, dfaces, drow, dcol};
+    for (void* q : ps) cudaFree(q);
     return 0;
 }
 

@@ -766,6 +766,42 @@ void orc_sim_backward(void* hv, void* tape, const double* dL_dx, const double* d
     });
 }
 
+// Output stage of Simulator::cuda_update_vbo (simulation.cu:196-231), headless.
+//   update_vbo_pos      (verlet.cu:119-127): pos4[i] = vec4(x[i], 1)
+//   compute_face_normal (verlet.cu:91-116):  fn[f] = normalize(cross(p1 - p0, p2 - p0)) of x_prev
+//   get_vertex_adjface  (simulation.cu:152-180): faces of each vertex, in face order
+//   compute_vbo_normal  (verlet.cu:163-181): vn[i] = normalize(sum of its faces' normals)
+// x are the positions after the step (x_cur_out), x_prev the ones the step started
+// from (x_cur_in: the reference computes normals from them).  Any output may be NULL.
+void orc_render(const float* x, const float* x_prev, int n, const uint32_t* faces, int nf, float* pos4,
+                float* vnormal, float* fnormal) {
+    if (pos4)
+        for (int i = 0; i < n; ++i) {
+            pos4[4 * i] = x[3 * i];
+            pos4[4 * i + 1] = x[3 * i + 1];
+            pos4[4 * i + 2] = x[3 * i + 2];
+            pos4[4 * i + 3] = 1.0f;
+        }
+    std::vector<V3<float>> fn(nf);
+    for (int f = 0; f < nf; ++f) {
+        const V3<float> p0 = cvt<float>(x_prev + 3 * (size_t)faces[3 * f]);
+        const V3<float> p1 = cvt<float>(x_prev + 3 * (size_t)faces[3 * f + 1]);
+        const V3<float> p2 = cvt<float>(x_prev + 3 * (size_t)faces[3 * f + 2]);
+        fn[f] = normalize(cross(p1 - p0, p2 - p0));
+        if (fnormal) { fnormal[3 * f] = fn[f].x; fnormal[3 * f + 1] = fn[f].y; fnormal[3 * f + 2] = fn[f].z; }
+    }
+    if (!vnormal) return;
+    std::vector<std::vector<uint32_t>> adj(n);
+    for (int f = 0; f < nf; ++f)
+        for (int j = 0; j < 3; ++j) adj[faces[3 * f + j]].push_back((uint32_t)f);
+    for (int i = 0; i < n; ++i) {
+        V3<float> v = mk<float>(0.0f, 0.0f, 0.0f);
+        for (uint32_t f : adj[i]) v = v + fn[f];
+        v = normalize(v);
+        vnormal[3 * i] = v.x; vnormal[3 * i + 1] = v.y; vnormal[3 * i + 2] = v.z;
+    }
+}
+
 // Reference spring topology (Springs::create_neigh + CSR_spring).  Two passes like
 // visg_springs_from_mesh: NULL arrays return the counts only.
 int orc_springs_from_mesh(const float* xyz, int nv, const uint32_t* tris, int nt, uint32_t* row0,

@@ -91,6 +91,10 @@ def lib():
         "visg_batch_set_state": (C.c_int, [_vp, C.c_int32, _fp, _fp, _fp]),
         "visg_batch_wait_positions": (C.c_int, [_vp]),
         "visg_read_positions_async": (C.c_int, [_vp, _vp]),
+        "visg_set_faces": (C.c_int, [_vp, _u32p, C.c_int32]),
+        "visg_render": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32]),
+        "visg_batch_set_faces": (C.c_int, [_vp, C.c_int32, _u32p, C.c_int32]),
+        "visg_batch_render": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32]),
         "visg_wait_positions": (C.c_int, [_vp]),
         "visg_batch_info": (C.c_int, [_vp, _i32p, _i64p, _i64p, _i64p]),
         "visg_batch_sync": (C.c_int, [_vp]),
@@ -215,6 +219,22 @@ class Simulator:
     def positions_device(self, dev_ptr: int):
         _check(lib().visg_get_positions(self.h, dev_ptr, 1))
 
+    def set_faces(self, faces):
+        """The cloth's triangles ((F, 3) vertex indices), for render()."""
+        f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+        self.n_faces = len(f)
+        _check(lib().visg_set_faces(self.h, _p(f, _u32p), len(f)))
+
+    def render(self, normals_of_previous: bool = True):
+        """The output stage of cuda_update_vbo: (pos4 (n, 4), vertex normals (n, 3),
+        face normals (F, 3)) as host arrays."""
+        pos4 = np.empty((self.n, 4), np.float32)
+        vn = np.empty((self.n, 3), np.float32)
+        fn = np.empty((max(getattr(self, "n_faces", 0), 1), 3), np.float32)
+        _check(lib().visg_render(self.h, pos4.ctypes.data, vn.ctypes.data, fn.ctypes.data, 0,
+                                 1 if normals_of_previous else 0))
+        return pos4, vn, fn[:getattr(self, "n_faces", 0)]
+
     def read_positions_async(self, out):
         """Enqueue the read of all positions into `out` ((n, 3) float32, ideally
         page-locked) behind the steps issued so far; returns at once."""
@@ -328,6 +348,23 @@ class BatchSimulator:
 
     def positions_device(self, dev_ptr: int, garment: int = -1):
         _check(lib().visg_batch_get_positions(self.h, garment, dev_ptr, 1))
+
+    def set_faces(self, garment: int, faces):
+        f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+        if not hasattr(self, "face_counts"):
+            self.face_counts = {}
+        self.face_counts[garment] = len(f)
+        _check(lib().visg_batch_set_faces(self.h, garment, _p(f, _u32p), len(f)))
+
+    def render(self, normals_of_previous: bool = True):
+        n = int(self.offsets[-1])
+        nf = sum(getattr(self, "face_counts", {}).values())
+        pos4 = np.empty((n, 4), np.float32)
+        vn = np.empty((n, 3), np.float32)
+        fn = np.empty((max(nf, 1), 3), np.float32)
+        _check(lib().visg_batch_render(self.h, pos4.ctypes.data, vn.ctypes.data, fn.ctypes.data, 0,
+                                       1 if normals_of_previous else 0))
+        return pos4, vn, fn[:nf]
 
     def read_positions_async(self, out):
         """Enqueue the read of every garment's positions (concatenated) into `out`

@@ -131,6 +131,15 @@ struct Engine {
     int2* d_cand = nullptr;            // split collision: queued candidates
     uint32_t* d_cand_count = nullptr;
     int* d_hitleaf = nullptr;          // query cache: first-hit leaf per vertex
+    // output stage: faces of each garment (local indices), and on the device all
+    // garments' faces with global indices, the vertex -> face CSR, the face normals
+    std::vector<std::vector<uint32_t>> gfaces;
+    uint32_t* d_faces = nullptr;
+    uint32_t* d_frow = nullptr;
+    uint32_t* d_fcol = nullptr;
+    float* d_fnorm = nullptr;
+    int64_t NF = 0;
+    bool prev_ok = false;  // the other buffer holds the positions the last step started from
     int split = 1;                     // collision in its own kernel (autotuned)
     float* d_stage = nullptr;  // 9*N floats
     uint32_t* h_status = nullptr;  // pinned: err, check0, check1
@@ -176,6 +185,7 @@ struct Engine {
             if (rb.copied[k]) cudaEventDestroy(rb.copied[k]);
         }
         if (rb.copy) cudaStreamDestroy(rb.copy);
+        free_faces();
         if (rb.h_err) cudaFreeHost(rb.h_err);
         destroy_graphs();
         if (d_sv_idx) cudaFree(d_sv_idx);
@@ -543,6 +553,7 @@ struct Engine {
     int step(int n) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         if (n < 0) return fail(VISG_ERR_INVALID_ARG, "nsteps < 0");
+        if (n > 0) prev_ok = true;
         while (n > 0) {
             if (p.use_graph && n >= chunk_steps) {
                 if (!chunk_exec[cur]) {
@@ -734,6 +745,74 @@ struct Engine {
         return VISG_OK;
     }
 
+    void free_faces() {
+        void* ps[] = {d_faces, d_frow, d_fcol, d_fnorm};
+        for (void* q : ps)
+            if (q) cudaFree(q);
+        d_faces = d_frow = d_fcol = nullptr;
+        d_fnorm = nullptr;
+        NF = 0;
+    }
+
+    // faces of garment g (local vertex indices); rebuilds the device face arrays and
+    // the vertex -> face CSR (get_vertex_adjface, simulation.cu:152-180: each vertex's
+    // faces in face order)
+    int set_faces(int g, const uint32_t* faces, int nf) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (g < 0 || g >= G) return fail(VISG_ERR_INVALID_ARG, "garment out of range");
+        if (nf < 0 || (nf > 0 && !faces)) return fail(VISG_ERR_INVALID_ARG, "faces is NULL or n_faces < 0");
+        const int64_t ng = voff[g + 1] - voff[g];
+        for (int64_t k = 0; k < 3 * (int64_t)nf; ++k)
+            if (faces[k] >= (uint64_t)ng) return fail(VISG_ERR_INVALID_ARG, "face vertex index out of range");
+        if (int r = sync()) return r;
+        gfaces.resize(G);
+        gfaces[g].assign(faces, faces + 3 * (size_t)nf);
+        int64_t nft = 0;
+        for (auto& f : gfaces) nft += (int64_t)f.size() / 3;
+        if (3 * nft >= (int64_t)0xffffffffu) return fail(VISG_ERR_INVALID_ARG, "too many faces");
+        std::vector<uint32_t> hf(3 * (size_t)nft + 3), row(N + 1, 0), col(3 * (size_t)nft + 1);
+        int64_t fo = 0;
+        for (int gg = 0; gg < G; ++gg) {
+            for (size_t k = 0; k < gfaces[gg].size(); ++k) hf[3 * fo + k] = (uint32_t)(voff[gg] + gfaces[gg][k]);
+            fo += (int64_t)gfaces[gg].size() / 3;
+        }
+        for (int64_t k = 0; k < 3 * nft; ++k) ++row[hf[k] + 1];
+        for (int64_t v = 0; v < N; ++v) row[v + 1] += row[v];
+        std::vector<uint32_t> fill(row.begin(), row.end() - 1);
+        for (int64_t f = 0; f < nft; ++f)
+            for (int j = 0; j < 3; ++j) col[fill[hf[3 * f + j]]++] = (uint32_t)f;
+        free_faces();
+        CU(cudaMalloc((void**)&d_faces, hf.size() * 4));
+        CU(cudaMalloc((void**)&d_frow, row.size() * 4));
+        CU(cudaMalloc((void**)&d_fcol, col.size() * 4));
+        CU(cudaMalloc((void**)&d_fnorm, (3 * (size_t)nft + 3) * 4));
+        CU(cudaMemcpy(d_faces, hf.data(), hf.size() * 4, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_frow, row.data(), row.size() * 4, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_fcol, col.data(), col.size() * 4, cudaMemcpyHostToDevice));
+        NF = nft;
+        return VISG_OK;
+    }
+
+    // the output stage of cuda_update_vbo (simulation.cu:196-231) into caller buffers:
+    // pos4 (N x 4), vertex normals (N x 3), face normals (F x 3); any may be NULL.
+    // Normals are of the positions the last step started from (the reference's
+    // choice) when `prev` is set and a step has run, else of the current positions.
+    int render(float* pos4, float* vn, float* fn, int on_device, int prev) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if ((vn || fn) && !d_frow) return fail(VISG_ERR_STATE, "normals need the faces (visg_set_faces)");
+        const float4* now = d_state[cur];
+        const float4* from = (prev && prev_ok) ? d_state[cur ^ 1] : d_state[cur];
+        float4* dpos = on_device ? (float4*)pos4 : (pos4 ? (float4*)d_stage : nullptr);
+        float* dvn = on_device ? vn : (vn ? d_stage + 4 * N : nullptr);
+        float* dfn = (on_device && fn) ? fn : d_fnorm;
+        CU(launch_render(now, from, N, d_faces, NF, d_frow, d_fcol, (vn || fn) ? dfn : nullptr, dpos, dvn, stream));
+        if (on_device) return VISG_OK;
+        if (pos4) CU(cudaMemcpyAsync(pos4, d_stage, (size_t)N * 16, cudaMemcpyDeviceToHost, stream));
+        if (vn) CU(cudaMemcpyAsync(vn, d_stage + 4 * N, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
+        if (fn && NF > 0) CU(cudaMemcpyAsync(fn, d_fnorm, (size_t)NF * 12, cudaMemcpyDeviceToHost, stream));
+        return sync();
+    }
+
     int get_positions(int g, float* out, int on_device) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
@@ -801,6 +880,7 @@ struct Engine {
         if (x) CU(cudaMemcpyAsync(sx, x, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
         if (xo) CU(cudaMemcpyAsync(sxo, xo, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
         if (nrm) CU(cudaMemcpyAsync(sn, nrm, (size_t)n * 12, cudaMemcpyHostToDevice, stream));
+        prev_ok = false;
         CU(launch_pack_state(d_state[cur] + 2 * v0, d_state[cur ^ 1] + 2 * v0, d_normal + v0, n, x ? sx : nullptr,
                              xo ? sxo : nullptr, nrm ? sn : nullptr, p.dt, step_params().drec,
                              step_params().dmax, d_wild, stream));
@@ -1177,6 +1257,17 @@ int visg_wait_positions(VisgSim* sim) {
     return sim->eng.wait_positions();
 }
 
+int visg_set_faces(VisgSim* sim, const uint32_t* faces, int32_t n_faces) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.set_faces(0, faces, n_faces);
+}
+
+int visg_render(VisgSim* sim, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
+                int32_t normals_of_previous) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.render(pos4, vertex_normals, face_normals, on_device, normals_of_previous);
+}
+
 int visg_get_state(VisgSim* sim, float* x, float* xo, float* n) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.get_state(-1, x, xo, n);
@@ -1306,6 +1397,17 @@ int visg_batch_read_positions_async(VisgBatch* b, float* out) {
 int visg_batch_wait_positions(VisgBatch* b) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.wait_positions();
+}
+
+int visg_batch_set_faces(VisgBatch* b, int32_t garment, const uint32_t* faces, int32_t n_faces) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.set_faces(garment, faces, n_faces);
+}
+
+int visg_batch_render(VisgBatch* b, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
+                      int32_t normals_of_previous) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.render(pos4, vertex_normals, face_normals, on_device, normals_of_previous);
 }
 
 int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]) {

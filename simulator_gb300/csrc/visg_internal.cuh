@@ -185,6 +185,12 @@ cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int6
                               const float* xo, const float* nrm, float dt, int drec, float dmax, uint32_t* wild,
                               cudaStream_t s);
 
+// output stage: pos4 = (x, 1) of st_now; fn = face normals of st_prev; vn = normalised
+// sums of each vertex's face normals (row/col: vertex -> face CSR).  NULL skips one.
+cudaError_t launch_render(const float4* st_now, const float4* st_prev, int64_t n, const uint32_t* faces, int64_t nf,
+                          const uint32_t* row, const uint32_t* col, float* fn, float4* pos4, float* vn,
+                          cudaStream_t s);
+
 // forget the collision margin of vertices [v0, v1) (their body moved)
 cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s);
 
