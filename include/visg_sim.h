@@ -298,6 +298,26 @@ int visg_springs_from_mesh(const float* xyz, int32_t n_vertices,
                            uint32_t* row0, VisgSpring* ent0, int32_t* n_ent0,
                            uint32_t* row1, VisgSpring* ent1, int32_t* n_ent1);
 
+/* ---- real-mesh inputs (host only, no GPU) ---------------------------------------------
+ * visg_obj_load reads a Wavefront OBJ as the reference's ObjLoader + Mesh::unified do
+ * (ObjLoader.cpp:14-137, Mesh.cpp:17-38), without textures and materials: "v", "vn"
+ * and triangle "f" records in the "a b c" and "a/t/n b/t/n c/t/n" forms (1-based; the
+ * first three corners of a face); each vertex's normal is the one named by the last
+ * face corner that uses it ((0, 0, 0) for an unused vertex).  visg_obj_get copies out
+ * n_vertices x 3 positions and normals and n_faces x 3 vertex indices (0-based; any
+ * pointer may be NULL); visg_obj_free releases the object. */
+typedef struct VisgObj VisgObj;
+int visg_obj_load(const char* path, VisgObj** out, int32_t* n_vertices, int32_t* n_faces);
+int visg_obj_get(const VisgObj* obj, float* xyz, float* normals, uint32_t* faces);
+void visg_obj_free(VisgObj* obj);
+/* Mesh::scale (about the vertex mean), Mesh::translate and Mesh::rotation (degrees,
+ * axis 0 = x, 1 = y, 2 = z, about the vertex mean) of Mesh.cpp:41-99, in place on
+ * n x 3 positions: the transforms the reference's demo applies to its garment and
+ * body (main.cpp:24-32). */
+int visg_mesh_scale(float* xyz, int32_t n, float s);
+int visg_mesh_translate(float* xyz, int32_t n, float dx, float dy, float dz);
+int visg_mesh_rotate(float* xyz, int32_t n, float angle_degrees, int32_t axis);
+
 /* ======================================================================== */
 /* Body LBVH build that allocates no device memory.                           */
 /* ======================================================================== */

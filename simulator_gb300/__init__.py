@@ -92,6 +92,12 @@ def lib():
         "visg_batch_wait_positions": (C.c_int, [_vp]),
         "visg_read_positions_async": (C.c_int, [_vp, _vp]),
         "visg_set_faces": (C.c_int, [_vp, _u32p, C.c_int32]),
+        "visg_obj_load": (C.c_int, [C.c_char_p, C.POINTER(_vp), _i32p, _i32p]),
+        "visg_obj_get": (C.c_int, [_vp, _fp, _fp, _u32p]),
+        "visg_obj_free": (None, [_vp]),
+        "visg_mesh_scale": (C.c_int, [_fp, C.c_int32, C.c_float]),
+        "visg_mesh_translate": (C.c_int, [_fp, C.c_int32, C.c_float, C.c_float, C.c_float]),
+        "visg_mesh_rotate": (C.c_int, [_fp, C.c_int32, C.c_float, C.c_int32]),
         "visg_render": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32]),
         "visg_batch_set_faces": (C.c_int, [_vp, C.c_int32, _u32p, C.c_int32]),
         "visg_batch_render": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32]),
@@ -452,3 +458,46 @@ def springs_from_mesh(xyz, tris):
     _check(lib().visg_springs_from_mesh(_p(xyz), nv, _p(tris, _u32p), nt, _p(r0, _u32p), e0.ctypes.data,
                                         C.byref(n0), _p(r1, _u32p), e1.ctypes.data, C.byref(n1)))
     return [SpringList(r0, e0), SpringList(r1, e1)]
+
+
+def load_obj(path: str):
+    """A Wavefront OBJ read as the reference's ObjLoader + Mesh::unified do:
+    (xyz (V, 3) float32, per-vertex normals (V, 3), triangles (F, 3) uint32)."""
+    h = _vp()
+    nv, nf = C.c_int32(), C.c_int32()
+    _check(lib().visg_obj_load(str(path).encode(), C.byref(h), C.byref(nv), C.byref(nf)))
+    try:
+        xyz = np.empty((nv.value, 3), np.float32)
+        nrm = np.empty((nv.value, 3), np.float32)
+        faces = np.empty((nf.value, 3), np.uint32)
+        _check(lib().visg_obj_get(h, _p(xyz), _p(nrm), _p(faces, _u32p)))
+    finally:
+        lib().visg_obj_free(h)
+    return xyz, nrm, faces
+
+
+def mesh_scale(xyz, s: float):
+    """Mesh::scale: (v - mean) * s, in place on a float32 (n, 3) array."""
+    _check(lib().visg_mesh_scale(_p(xyz), len(xyz), s))
+    return xyz
+
+
+def mesh_translate(xyz, dx: float, dy: float, dz: float):
+    _check(lib().visg_mesh_translate(_p(xyz), len(xyz), dx, dy, dz))
+    return xyz
+
+
+def mesh_rotate(xyz, angle_degrees: float, axis: int):
+    """Mesh::rotation about the vertex mean; axis 0 = x, 1 = y, 2 = z."""
+    _check(lib().visg_mesh_rotate(_p(xyz), len(xyz), angle_degrees, axis))
+    return xyz
+
+
+def write_obj(path: str, xyz, faces=None):
+    """Positions (and triangles, 0-based) as a Wavefront OBJ ("v" and "f a b c")."""
+    with open(path, "w") as f:
+        for p in np.asarray(xyz, np.float32):
+            f.write(f"v {p[0]:.9g} {p[1]:.9g} {p[2]:.9g}\n")
+        if faces is not None:
+            for t in np.asarray(faces, np.int64):
+                f.write(f"f {t[0] + 1} {t[1] + 1} {t[2] + 1}\n")

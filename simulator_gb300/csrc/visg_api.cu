@@ -27,6 +27,13 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
+}  // namespace
+
+// the message visg_last_error returns, for the host-only translation units
+void visg::set_last_error(const char* msg) { g_err = msg; }
+
+namespace {
+
 int cuda_fail(cudaError_t e, const char* what) {
     return fail(e == cudaErrorMemoryAllocation ? VISG_ERR_OOM : VISG_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));

@@ -40,6 +40,8 @@
 
 namespace visg {
 
+void set_last_error(const char* msg);  // what visg_last_error returns next
+
 constexpr uint32_t PIN_BIT = 0x80000000u;
 constexpr uint32_t ROW_MASK = 0x7fffffffu;
 constexpr uint32_t END_MASK = 0x3fffffffu;
