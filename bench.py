@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-garment loop")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-moving", action="store_true", help="skip the moving-body plain configs")
+    ap.add_argument("--moving-only", action="store_true",
+                    help="only the moving-body plain configs (one JSON object; for profiling the LBVH rebuild)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--launch", default=None, help="block,ctas_per_sm instead of autotuning (profiling runs)")
@@ -301,6 +303,10 @@ def main():
     sampler = ClockSampler(phys)
 
     params = scenes.physics_params(args.substeps)
+    if args.moving_only:
+        out = moving_body_configs(vs, scenes, torch, params, torch.cuda.current_stream(), args.steps, args.warmup)
+        print(json.dumps({"moving_body_configs": out}), flush=True)
+        return 0
     if args.stage is not None:
         params.stage_neighbours = args.stage
     items, nv, ne, nt = build_workload(args.garments, args.seed + rank)
