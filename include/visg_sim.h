@@ -160,6 +160,13 @@ int visg_get_positions(VisgSim* sim, float* out, int32_t on_device);
 int visg_set_faces(VisgSim* sim, const uint32_t* faces, int32_t n_faces);
 int visg_render(VisgSim* sim, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
                 int32_t normals_of_previous);
+/* visg_render plus, per vertex, the colour the reference's fragment shader gives it
+ * (src/shaders/sh.frag:13-55, evaluated at the vertex normal instead of per fragment):
+ * the order-2 spherical-harmonic irradiance polynomial with its "old town square"
+ * coefficients, term by term in the shader's order, times object_rgb (its texture
+ * lookup is dropped; ambient and specular are zero there).  colors: n_vertices x 3. */
+int visg_render_shaded(VisgSim* sim, float* pos4, float* vertex_normals, float* colors, const float object_rgb[3],
+                       int32_t on_device, int32_t normals_of_previous);
 
 /* Pipelined read-back (no counterpart in the reference, whose cuda_update_vbo
  * copies synchronously every frame): enqueues, behind the steps issued so far, the
@@ -255,6 +262,8 @@ int visg_batch_set_state(VisgBatch* b, int32_t garment, const float* x, const fl
 int visg_batch_set_faces(VisgBatch* b, int32_t garment, const uint32_t* faces, int32_t n_faces);
 int visg_batch_render(VisgBatch* b, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
                       int32_t normals_of_previous);
+int visg_batch_render_shaded(VisgBatch* b, float* pos4, float* vertex_normals, float* colors,
+                             const float object_rgb[3], int32_t on_device, int32_t normals_of_previous);
 /* visg_read_positions_async / visg_wait_positions over all garments (concatenated). */
 int visg_batch_read_positions_async(VisgBatch* b, float* out);
 int visg_batch_wait_positions(VisgBatch* b);
@@ -297,6 +306,19 @@ int visg_springs_from_mesh(const float* xyz, int32_t n_vertices,
                            const uint32_t* tris, int32_t n_tris,
                            uint32_t* row0, VisgSpring* ent0, int32_t* n_ent0,
                            uint32_t* row1, VisgSpring* ent1, int32_t* n_ent1);
+/* visg_springs_from_mesh for a multi-piece garment (the reference's
+ * SINGLE_LAYER_BOUNDARY, Springs::get_cloth_boundary_spring and
+ * get_boundary_boundary_spring, spring.cpp:98-209): the vertices come in groups
+ * (piece, its boundary, piece, its boundary, ...; n_groups even, sizes as
+ * visg_obj_groups gives them).  Each boundary vertex is joined both ways to its
+ * nearest vertex of its own piece, and the pieces' vertices behind two boundary
+ * vertices that are nearest neighbours across boundaries (closer than 50 times the
+ * mean boundary-to-piece distance, and apart) are joined: the seams.  These are
+ * appended to the structure list after the faces' springs, in the reference's order;
+ * nearest neighbours follow the rules of the reference's kd-tree (ties included). */
+int visg_springs_from_mesh_sewn(const float* xyz, int32_t n_vertices, const uint32_t* tris, int32_t n_tris,
+                                const int32_t* group_sizes, int32_t n_groups, uint32_t* row0, VisgSpring* ent0,
+                                int32_t* n0, uint32_t* row1, VisgSpring* ent1, int32_t* n1);
 
 /* ---- real-mesh inputs (host only, no GPU) ---------------------------------------------
  * visg_obj_load reads a Wavefront OBJ as the reference's ObjLoader + Mesh::unified do
@@ -309,6 +331,10 @@ int visg_springs_from_mesh(const float* xyz, int32_t n_vertices,
 typedef struct VisgObj VisgObj;
 int visg_obj_load(const char* path, VisgObj** out, int32_t* n_vertices, int32_t* n_faces);
 int visg_obj_get(const VisgObj* obj, float* xyz, float* normals, uint32_t* faces);
+/* The vertex groups of a multi-piece garment: the "# object NAME" records, each sized
+ * by the "# N vertices" record after it (ObjLoader.cpp:33-40), in file order: piece 0,
+ * its boundary, piece 1, its boundary, ...  sizes may be NULL (count only). */
+int visg_obj_groups(const VisgObj* obj, int32_t* sizes, int32_t* n_groups);
 void visg_obj_free(VisgObj* obj);
 /* Mesh::scale (about the vertex mean), Mesh::translate and Mesh::rotation (degrees,
  * axis 0 = x, 1 = y, 2 = z, about the vertex mean) of Mesh.cpp:41-99, in place on

@@ -51,6 +51,7 @@ def lib():
         L.orc_springs_from_mesh.argtypes = [_fp, C.c_int, _u32p, C.c_int, _u32p, C.c_void_p, _i32p,
                                             _u32p, C.c_void_p, _i32p]
         L.orc_render.argtypes = [_fp, _fp, C.c_int, _u32p, C.c_int, _fp, _fp, _fp]
+        L.orc_sh_shade.argtypes = [_fp, C.c_int, _fp, _fp]
         _lib = L
     return _lib
 
@@ -198,6 +199,15 @@ def render(x, x_prev, faces):
     fn = np.zeros((nf, 3), np.float32)
     lib().orc_render(ptr(x, _fp), ptr(xp, _fp), n, ptr(f, _u32p), nf, ptr(pos4, _fp), ptr(vn, _fp), ptr(fn, _fp))
     return pos4, vn, fn
+
+
+def sh_shade(normals, rgb):
+    """The reference's SH fragment shader restated at each normal: colours (n, 3)."""
+    nrm = np.ascontiguousarray(normals, np.float32)
+    c = np.ascontiguousarray(rgb, np.float32)
+    out = np.zeros((len(nrm), 3), np.float32)
+    lib().orc_sh_shade(ptr(nrm, _fp), len(nrm), ptr(c, _fp), ptr(out, _fp))
+    return out
 
 
 def springs_from_mesh(xyz, tris):

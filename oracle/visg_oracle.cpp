@@ -802,6 +802,37 @@ void orc_render(const float* x, const float* x_prev, int n, const uint32_t* face
     }
 }
 
+// The reference's fragment shader (src/shaders/sh.frag:13-55) at each vertex normal:
+// diffuse = C1 L22 (x x - y y) + C3 L20 z z + C4 L00 - C5 L20 + 2 C1 L2m2 x y
+//           + 2 C1 L21 x y + 2 C1 L2m1 y z + 2 C2 L11 x + 2 C2 L1m1 y + 2 C2 L10 z,
+// term by term left to right on normalize(n); colour = ((0 + diffuse * 1) + 0) * rgb.
+void orc_sh_shade(const float* normals, int n, const float* rgb, float* out) {
+    const float C1 = 0.429043f, C2 = 0.511664f, C3 = 0.743125f, C4 = 0.886227f, C5 = 0.247708f;
+    const V3<float> L00 = mk(0.87f, 0.87f, 0.86f), L1m1 = mk(0.17f, 0.24f, 0.31f), L10 = mk(0.03f, 0.03f, 0.03f);
+    const V3<float> L11 = mk(-0.004f, -0.03f, -0.05f), L2m2 = mk(-0.12f, -0.12f, -0.11f);
+    const V3<float> L2m1 = mk(0.003f, 0.003f, 0.007f), L20 = mk(-0.03f, -0.02f, -0.02f);
+    const V3<float> L21 = mk(-0.08f, -0.08f, -0.09f), L22 = mk(-0.16f, -0.19f, -0.22f);
+    const float c1x2 = 2.0f * C1, c2x2 = 2.0f * C2;
+    for (int i = 0; i < n; ++i) {
+        const V3<float> t = normalize(cvt<float>(normals + 3 * (size_t)i));
+        V3<float> d = (C1 * L22) * (t.x * t.x - t.y * t.y);
+        d = d + ((C3 * L20) * t.z) * t.z;
+        d = d + C4 * L00;
+        d = d - C5 * L20;
+        d = d + ((c1x2 * L2m2) * t.x) * t.y;
+        d = d + ((c1x2 * L21) * t.x) * t.y;
+        d = d + ((c1x2 * L2m1) * t.y) * t.z;
+        d = d + (c2x2 * L11) * t.x;
+        d = d + (c2x2 * L1m1) * t.y;
+        d = d + (c2x2 * L10) * t.z;
+        d = d * 1.0f;
+        const V3<float> r = (mk(0.0f, 0.0f, 0.0f) + d) + mk(0.0f, 0.0f, 0.0f);
+        out[3 * i] = r.x * rgb[0];
+        out[3 * i + 1] = r.y * rgb[1];
+        out[3 * i + 2] = r.z * rgb[2];
+    }
+}
+
 // Reference spring topology (Springs::create_neigh + CSR_spring).  Two passes like
 // visg_springs_from_mesh: NULL arrays return the counts only.
 int orc_springs_from_mesh(const float* xyz, int nv, const uint32_t* tris, int nt, uint32_t* row0,

@@ -95,10 +95,15 @@ def lib():
         "visg_obj_load": (C.c_int, [C.c_char_p, C.POINTER(_vp), _i32p, _i32p]),
         "visg_obj_get": (C.c_int, [_vp, _fp, _fp, _u32p]),
         "visg_obj_free": (None, [_vp]),
+        "visg_obj_groups": (C.c_int, [_vp, _i32p, _i32p]),
+        "visg_springs_from_mesh_sewn": (C.c_int, [_fp, C.c_int32, _u32p, C.c_int32, _i32p, C.c_int32, _u32p,
+                                                  _vp, _i32p, _u32p, _vp, _i32p]),
         "visg_mesh_scale": (C.c_int, [_fp, C.c_int32, C.c_float]),
         "visg_mesh_translate": (C.c_int, [_fp, C.c_int32, C.c_float, C.c_float, C.c_float]),
         "visg_mesh_rotate": (C.c_int, [_fp, C.c_int32, C.c_float, C.c_int32]),
         "visg_render": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32]),
+        "visg_render_shaded": (C.c_int, [_vp, _vp, _vp, _vp, _fp, C.c_int32, C.c_int32]),
+        "visg_batch_render_shaded": (C.c_int, [_vp, _vp, _vp, _vp, _fp, C.c_int32, C.c_int32]),
         "visg_batch_set_faces": (C.c_int, [_vp, C.c_int32, _u32p, C.c_int32]),
         "visg_batch_render": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32]),
         "visg_wait_positions": (C.c_int, [_vp]),
@@ -240,6 +245,16 @@ class Simulator:
         _check(lib().visg_render(self.h, pos4.ctypes.data, vn.ctypes.data, fn.ctypes.data, 0,
                                  1 if normals_of_previous else 0))
         return pos4, vn, fn[:getattr(self, "n_faces", 0)]
+
+    def render_shaded(self, object_rgb=(1.0, 1.0, 1.0), normals_of_previous: bool = True):
+        """(pos4, vertex normals, SH-shaded colours (n, 3)) as host arrays."""
+        pos4 = np.empty((self.n, 4), np.float32)
+        vn = np.empty((self.n, 3), np.float32)
+        col = np.empty((self.n, 3), np.float32)
+        rgb = np.ascontiguousarray(object_rgb, np.float32)
+        _check(lib().visg_render_shaded(self.h, pos4.ctypes.data, vn.ctypes.data, col.ctypes.data, _p(rgb), 0,
+                                        1 if normals_of_previous else 0))
+        return pos4, vn, col
 
     def read_positions_async(self, out):
         """Enqueue the read of all positions into `out` ((n, 3) float32, ideally
@@ -501,3 +516,36 @@ def write_obj(path: str, xyz, faces=None):
         if faces is not None:
             for t in np.asarray(faces, np.int64):
                 f.write(f"f {t[0] + 1} {t[1] + 1} {t[2] + 1}\n")
+
+
+def obj_groups(path: str):
+    """Vertex group sizes of a multi-piece garment OBJ ("# object" / "# N vertices")."""
+    h = _vp()
+    nv, nf, ng = C.c_int32(), C.c_int32(), C.c_int32()
+    _check(lib().visg_obj_load(str(path).encode(), C.byref(h), C.byref(nv), C.byref(nf)))
+    try:
+        _check(lib().visg_obj_groups(h, None, C.byref(ng)))
+        g = np.zeros(ng.value, np.int32)
+        _check(lib().visg_obj_groups(h, _p(g, _i32p), C.byref(ng)))
+    finally:
+        lib().visg_obj_free(h)
+    return g
+
+
+def springs_from_mesh_sewn(xyz, tris, group_sizes):
+    """springs_from_mesh plus the seams of a multi-piece garment (the reference's
+    SINGLE_LAYER_BOUNDARY): group_sizes = piece, boundary, piece, boundary, ..."""
+    from .scenes import SPRING_DTYPE, SpringList
+    xyz = _f32(xyz)
+    tris = np.ascontiguousarray(tris, np.uint32)
+    g = np.ascontiguousarray(group_sizes, np.int32)
+    nv, nt = len(xyz), len(tris)
+    n0, n1 = C.c_int32(), C.c_int32()
+    _check(lib().visg_springs_from_mesh_sewn(_p(xyz), nv, _p(tris, _u32p), nt, _p(g, _i32p), len(g), None, None,
+                                             C.byref(n0), None, None, C.byref(n1)))
+    r0, r1 = np.zeros(nv + 1, np.uint32), np.zeros(nv + 1, np.uint32)
+    e0, e1 = np.zeros(n0.value, SPRING_DTYPE), np.zeros(n1.value, SPRING_DTYPE)
+    _check(lib().visg_springs_from_mesh_sewn(_p(xyz), nv, _p(tris, _u32p), nt, _p(g, _i32p), len(g),
+                                             _p(r0, _u32p), e0.ctypes.data, C.byref(n0), _p(r1, _u32p),
+                                             e1.ctypes.data, C.byref(n1)))
+    return [SpringList(r0, e0), SpringList(r1, e1)]

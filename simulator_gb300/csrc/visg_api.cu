@@ -148,7 +148,7 @@ struct Engine {
     int64_t NF = 0;
     bool prev_ok = false;  // the other buffer holds the positions the last step started from
     int split = 1;                     // collision in its own kernel (autotuned)
-    float* d_stage = nullptr;  // 9*N floats
+    float* d_stage = nullptr;  // 10*N floats
     uint32_t* h_status = nullptr;  // pinned: err, check0, check1
     int cur = 0;
     int block = 256, grid = 0;
@@ -409,7 +409,7 @@ struct Engine {
         arena.want(&d_cand, (size_t)N + 1);
         arena.want(&d_cand_count, 4);
         arena.want(&d_hitleaf, (size_t)N + 1);
-        arena.want(&d_stage, 9 * (size_t)N + 4);
+        arena.want(&d_stage, 10 * (size_t)N + 4);
         bvh.resize(G);
         for (int g = 0; g < G; ++g)
             if (gin[g].nt > 0) bvh[g].plan(arena, gin[g].nv, gin[g].nt, !gin[g].bnrm.empty());
@@ -804,18 +804,22 @@ struct Engine {
     // pos4 (N x 4), vertex normals (N x 3), face normals (F x 3); any may be NULL.
     // Normals are of the positions the last step started from (the reference's
     // choice) when `prev` is set and a step has run, else of the current positions.
-    int render(float* pos4, float* vn, float* fn, int on_device, int prev) {
+    int render(float* pos4, float* vn, float* fn, float* colour, const float* rgb, int on_device, int prev) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
-        if ((vn || fn) && !d_frow) return fail(VISG_ERR_STATE, "normals need the faces (visg_set_faces)");
+        if ((vn || fn || colour) && !d_frow) return fail(VISG_ERR_STATE, "normals need the faces (visg_set_faces)");
+        if (colour && !rgb) return fail(VISG_ERR_INVALID_ARG, "shaded colours need the object colour");
         const float4* now = d_state[cur];
         const float4* from = (prev && prev_ok) ? d_state[cur ^ 1] : d_state[cur];
         float4* dpos = on_device ? (float4*)pos4 : (pos4 ? (float4*)d_stage : nullptr);
         float* dvn = on_device ? vn : (vn ? d_stage + 4 * N : nullptr);
+        float* dcol = on_device ? colour : (colour ? d_stage + 7 * N : nullptr);
         float* dfn = (on_device && fn) ? fn : d_fnorm;
-        CU(launch_render(now, from, N, d_faces, NF, d_frow, d_fcol, (vn || fn) ? dfn : nullptr, dpos, dvn, stream));
+        CU(launch_render(now, from, N, d_faces, NF, d_frow, d_fcol, (vn || fn || colour) ? dfn : nullptr, dpos, dvn,
+                         dcol, rgb, stream));
         if (on_device) return VISG_OK;
         if (pos4) CU(cudaMemcpyAsync(pos4, d_stage, (size_t)N * 16, cudaMemcpyDeviceToHost, stream));
         if (vn) CU(cudaMemcpyAsync(vn, d_stage + 4 * N, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
+        if (colour) CU(cudaMemcpyAsync(colour, d_stage + 7 * N, (size_t)N * 12, cudaMemcpyDeviceToHost, stream));
         if (fn && NF > 0) CU(cudaMemcpyAsync(fn, d_fnorm, (size_t)NF * 12, cudaMemcpyDeviceToHost, stream));
         return sync();
     }
@@ -1272,7 +1276,13 @@ int visg_set_faces(VisgSim* sim, const uint32_t* faces, int32_t n_faces) {
 int visg_render(VisgSim* sim, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
                 int32_t normals_of_previous) {
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
-    return sim->eng.render(pos4, vertex_normals, face_normals, on_device, normals_of_previous);
+    return sim->eng.render(pos4, vertex_normals, face_normals, nullptr, nullptr, on_device, normals_of_previous);
+}
+
+int visg_render_shaded(VisgSim* sim, float* pos4, float* vertex_normals, float* colors, const float object_rgb[3],
+                       int32_t on_device, int32_t normals_of_previous) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.render(pos4, vertex_normals, nullptr, colors, object_rgb, on_device, normals_of_previous);
 }
 
 int visg_get_state(VisgSim* sim, float* x, float* xo, float* n) {
@@ -1414,7 +1424,13 @@ int visg_batch_set_faces(VisgBatch* b, int32_t garment, const uint32_t* faces, i
 int visg_batch_render(VisgBatch* b, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
                       int32_t normals_of_previous) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
-    return b->eng.render(pos4, vertex_normals, face_normals, on_device, normals_of_previous);
+    return b->eng.render(pos4, vertex_normals, face_normals, nullptr, nullptr, on_device, normals_of_previous);
+}
+
+int visg_batch_render_shaded(VisgBatch* b, float* pos4, float* vertex_normals, float* colors,
+                             const float object_rgb[3], int32_t on_device, int32_t normals_of_previous) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.render(pos4, vertex_normals, nullptr, colors, object_rgb, on_device, normals_of_previous);
 }
 
 int visg_batch_set_vertex(VisgBatch* b, int32_t garment, uint32_t idx, const float xyz[3]) {

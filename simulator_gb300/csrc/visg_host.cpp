@@ -15,7 +15,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/visg_sim.h"
@@ -47,10 +49,11 @@ void emit(const std::vector<std::vector<uint32_t>>& nb, const float* xyz, uint32
     if (count) *count = (int32_t)c;
 }
 
-}  // namespace
-
-extern "C" int visg_springs_from_mesh(const float* xyz, int32_t nv, const uint32_t* tris, int32_t nt, uint32_t* row0,
-                                      VisgSpring* ent0, int32_t* n0, uint32_t* row1, VisgSpring* ent1, int32_t* n1) {
+// the structure and bend lists of create_neigh (spring.cpp:286-353); `seam` are the
+// extra structure springs of a multi-piece garment, appended after the faces' ones
+int springs_impl(const float* xyz, int32_t nv, const uint32_t* tris, int32_t nt,
+                 const std::vector<std::pair<uint32_t, uint32_t>>& seam, uint32_t* row0, VisgSpring* ent0,
+                 int32_t* n0, uint32_t* row1, VisgSpring* ent1, int32_t* n1) {
     if (!xyz || nv <= 0 || (nt > 0 && !tris) || nt < 0) return VISG_ERR_INVALID_ARG;
     for (int64_t k = 0; k < 3 * (int64_t)nt; ++k)
         if (tris[k] >= (uint32_t)nv) return VISG_ERR_INVALID_ARG;
@@ -87,6 +90,7 @@ extern "C" int visg_springs_from_mesh(const float* xyz, int32_t nv, const uint32
         insert(f[0], f[2], f[1]);
         insert(f[1], f[2], f[0]);
     }
+    for (auto& pr : seam) n1v[pr.first].push_back(pr.second);
     for (auto& pr : pairs) {
         n2v[pr.first].push_back(pr.second);
         n2v[pr.second].push_back(pr.first);
@@ -94,4 +98,31 @@ extern "C" int visg_springs_from_mesh(const float* xyz, int32_t nv, const uint32
     emit(n1v, xyz, row0, ent0, n0);
     emit(n2v, xyz, row1, ent1, n1);
     return VISG_OK;
+}
+
+}  // namespace
+
+namespace visg {
+int sewing_pairs(const float* xyz, int64_t n, const int32_t* sizes, int32_t n_groups,
+                 std::vector<std::pair<uint32_t, uint32_t>>& out, std::string& err);  // visg_mesh.cpp
+void set_last_error(const char* msg);                                               // visg_api.cu
+}  // namespace visg
+
+extern "C" int visg_springs_from_mesh(const float* xyz, int32_t nv, const uint32_t* tris, int32_t nt, uint32_t* row0,
+                                      VisgSpring* ent0, int32_t* n0, uint32_t* row1, VisgSpring* ent1, int32_t* n1) {
+    return springs_impl(xyz, nv, tris, nt, {}, row0, ent0, n0, row1, ent1, n1);
+}
+
+extern "C" int visg_springs_from_mesh_sewn(const float* xyz, int32_t nv, const uint32_t* tris, int32_t nt,
+                                           const int32_t* group_sizes, int32_t n_groups, uint32_t* row0,
+                                           VisgSpring* ent0, int32_t* n0, uint32_t* row1, VisgSpring* ent1,
+                                           int32_t* n1) {
+    if (!xyz || nv <= 0 || !group_sizes) return VISG_ERR_INVALID_ARG;
+    std::vector<std::pair<uint32_t, uint32_t>> seam;
+    std::string err;
+    if (visg::sewing_pairs(xyz, nv, group_sizes, n_groups, seam, err)) {
+        visg::set_last_error(err.c_str());
+        return VISG_ERR_INVALID_ARG;
+    }
+    return springs_impl(xyz, nv, tris, nt, seam, row0, ent0, n0, row1, ent1, n1);
 }

@@ -189,9 +189,10 @@ cudaError_t launch_pack_state(float4* state, float4* other, float4* normal, int6
 
 // output stage: pos4 = (x, 1) of st_now; fn = face normals of st_prev; vn = normalised
 // sums of each vertex's face normals (row/col: vertex -> face CSR).  NULL skips one.
+// colour (with rgb, the object colour): the SH-shaded colour of each vertex normal
 cudaError_t launch_render(const float4* st_now, const float4* st_prev, int64_t n, const uint32_t* faces, int64_t nf,
-                          const uint32_t* row, const uint32_t* col, float* fn, float4* pos4, float* vn,
-                          cudaStream_t s);
+                          const uint32_t* row, const uint32_t* col, float* fn, float4* pos4, float* vn, float* colour,
+                          const float* rgb, cudaStream_t s);
 
 // forget the collision margin of vertices [v0, v1) (their body moved)
 cudaError_t launch_clear_margin(float4* state, int64_t v0, int64_t v1, cudaStream_t s);

@@ -8,7 +8,8 @@ Reads both meshes (visg_obj_load), applies the demo's placement with
 --reference-pose (the garment rotated 90 degrees about x and -4 about z, scaled by
 3.33 and raised by (0, 1.98, 0.02); the body scaled by 3.226 and raised by
 (0, 1.8, 0)), builds the reference's two spring lists from the garment's triangles,
-and steps the simulator with the reference's constants, writing the garment as
+(sewing the pieces of a multi-piece garment, as the reference does for
+SINGLE_LAYER_BOUNDARY meshes) and steps the simulator with the reference's constants, writing the garment as
 an OBJ every --every steps (positions and triangles) and printing the throughput.
 """
 from __future__ import annotations
@@ -40,7 +41,8 @@ def main(argv=None):
         vs.mesh_translate(cloth, 0, 1.98, 0.02)
         vs.mesh_scale(body, 3.226)
         vs.mesh_translate(body, 0, 1.8, 0)
-    lists = vs.springs_from_mesh(cloth, cf)
+    groups = vs.obj_groups(a.cloth)  # a multi-piece garment ("# object" groups) is sewn
+    lists = vs.springs_from_mesh_sewn(cloth, cf, groups) if len(groups) >= 2 else vs.springs_from_mesh(cloth, cf)
     sim = vs.Simulator(cloth, lists, body, bf, bn, params=vs.reference_params(2))
     sim.set_faces(cf)
     os.makedirs(a.out, exist_ok=True)

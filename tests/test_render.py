@@ -134,3 +134,50 @@ def test_render_requires_faces_for_normals():
         g.render()
     with pytest.raises(vs.VisgError):
         g.set_faces(np.array([[0, 1, len(cloth.xyz)]], np.uint32))
+
+
+def np_sh(normals, rgb):
+    """The SH fragment shader (sh.frag:13-55), float32, term by term in its order."""
+    C1, C2, C3, C4, C5 = F(0.429043), F(0.511664), F(0.743125), F(0.886227), F(0.247708)
+    L = {k: np.array(v, F) for k, v in dict(L00=(0.87, 0.87, 0.86), L1m1=(0.17, 0.24, 0.31), L10=(0.03, 0.03, 0.03),
+                                            L11=(-0.004, -0.03, -0.05), L2m2=(-0.12, -0.12, -0.11),
+                                            L2m1=(0.003, 0.003, 0.007), L20=(-0.03, -0.02, -0.02),
+                                            L21=(-0.08, -0.08, -0.09), L22=(-0.16, -0.19, -0.22)).items()}
+    n = normals.astype(F)
+    d = (n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]
+    t = n * (F(1) / np.sqrt(d))[:, None]
+    x, y, z = t[:, :1], t[:, 1:2], t[:, 2:3]
+    a, b = F(2) * C1, F(2) * C2
+    r = (C1 * L["L22"]) * (x * x - y * y)
+    r = r + ((C3 * L["L20"]) * z) * z
+    r = r + C4 * L["L00"]
+    r = r - C5 * L["L20"]
+    r = r + ((a * L["L2m2"]) * x) * y
+    r = r + ((a * L["L21"]) * x) * y
+    r = r + ((a * L["L2m1"]) * y) * z
+    r = r + (b * L["L11"]) * x
+    r = r + (b * L["L1m1"]) * y
+    r = r + (b * L["L10"]) * z
+    r = (F(0) + r * F(1)) + F(0)
+    return r * np.asarray(rgb, F)
+
+
+def test_oracle_sh_shade_matches_float32_restatement():
+    rng = np.random.default_rng(9)
+    nrm = rng.normal(0, 1, (500, 3)).astype(F)
+    rgb = F([0.9, 0.7, 0.5])
+    assert same(ffi.sh_shade(nrm, rgb), np_sh(nrm, rgb))
+
+
+@pytest.mark.gpu
+def test_render_shaded_matches_oracle():
+    import simulator_gb300 as vs
+    cloth, body, p = draped()
+    g = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=p, pinned=cloth.pinned)
+    g.set_faces(cloth.faces)
+    g.simulate(30)
+    rgb = (0.8, 0.6, 0.4)
+    pos4, vn, col = g.render_shaded(rgb)
+    q4, qn, _ = g.render()
+    assert same(pos4, q4) and same(vn, qn)
+    assert same(col, ffi.sh_shade(vn, rgb))
