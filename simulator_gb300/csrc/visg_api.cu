@@ -412,7 +412,10 @@ struct Engine {
         arena.want(&d_stage, 10 * (size_t)N + 4);
         bvh.resize(G);
         for (int g = 0; g < G; ++g)
-            if (gin[g].nt > 0) bvh[g].plan(arena, gin[g].nv, gin[g].nt, !gin[g].bnrm.empty());
+            if (gin[g].nt > 0) {
+                bvh[g].plan(arena, gin[g].nv, gin[g].nt, !gin[g].bnrm.empty());
+                bvh[g].coherent = true;  // rebuilt in place: the last build's order is at hand
+            }
         CU(arena.commit());
         // upload
         std::vector<float4> st(2 * (size_t)N);

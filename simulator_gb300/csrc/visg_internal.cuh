@@ -68,7 +68,7 @@ struct __align__(16) BvhRoot {
     int root;      // root internal node, -1 when there are fewer than two leaves
     int n_leaves;  // T' (after de-duplication)
     int n_tris;    // T
-    int pad;
+    int perm_valid;  // the sort buffers hold the last build's sorted codes and permutation
     float4 frame_lo, frame_hi;  // Morton frame: identity box U every expanded triangle box
     float4 top_lo, top_hi;      // box of the root node (identity U children), or of the only leaf
     uint32_t acc[8];            // order-preserving accumulators of the frame (min xyz, max xyz)
@@ -97,6 +97,7 @@ struct BvhBuffers {
     int nv = 0, nt = 0;        // body vertices, triangles
     int tiles_sort = 0;        // look-back tiles of one radix pass
     bool has_normals = false;
+    bool coherent = false;     // reuse the last build's order when the codes still sort the same
     float* xyz_in = nullptr;   // nv*3 staging (upload target)
     float* nrm_in = nullptr;   // nv*3 staging
     float4* verts = nullptr;   // nv, thickness push applied

@@ -4,13 +4,16 @@
 // body with a device->host->device round trip: expanded boxes and Morton codes on
 // the GPU, std::sort + duplicate removal on the CPU, then Karras internal nodes and
 // an atomic-counter refit on the GPU.  Here the whole build stays on the device,
-// in nine stream-ordered kernels, so it can run every step and be captured in a
+// in up to ten stream-ordered kernels, so it can run every step and be captured in a
 // CUDA graph:
 //   k_body_prep   vertex_extend (Mesh.cpp:101-117): v += thickness * n
 //   k_tri_boxes   expanded triangle boxes (primitive.cu:79-91) + the Morton frame
 //                 (identity box U all boxes) by warp-shuffle min/max reduction
 //   k_morton      Morton code of each box centroid in the frame (bvh.cu:20-41,71-79;
 //                 bbox.h:97-127) + the digit histograms of all four radix passes
+//   k_coherence   (bodies rebuilt every step) is the last build's permutation still
+//                 the stable order of the new codes?  Then the radix passes exit at
+//                 once; if every code is unchanged too, so does k_unique
 //   k_sort_pass   x4: stable LSD radix pass, 8-bit digits, decoupled look-back
 //                 (ties keep triangle order, i.e. sort by (code, triangle))
 //   k_unique      keep the first triangle of every distinct code
@@ -41,10 +44,17 @@ constexpr int SORT_ITEMS = 8;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 2048
 constexpr int RADIX = 256;
 constexpr int PASSES = 4;
+static_assert(PASSES % 2 == 0, "the last pass writes keys[1] / vals[1], which k_coherence reads");
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_PREFIX = 2u << 30;
 constexpr uint32_t ST_VALUE = (1u << 30) - 1u;
 constexpr int SPIN_LIMIT = 1 << 22;
+// rebuild mode word (zero before every build): what k_coherence found
+constexpr uint32_t M_RAN = 1u;       // the check ran (else every pass does its work)
+constexpr uint32_t M_UNSORTED = 2u;  // the last permutation does not sort the new codes
+constexpr uint32_t M_CHANGED = 4u;   // some code changed
+__device__ __forceinline__ bool skip_sort(uint32_t m) { return (m & M_RAN) && !(m & M_UNSORTED); }
+__device__ __forceinline__ bool skip_unique(uint32_t m) { return (m & M_RAN) && !(m & (M_UNSORTED | M_CHANGED)); }
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
     return *reinterpret_cast<const volatile uint32_t*>(p);
@@ -190,13 +200,47 @@ k_morton(const float4* __restrict__ tri_box, int nt, BvhRoot* root, uint32_t* __
     }
 }
 
+// Temporal coherence of a rebuild.  keys1/vals1 hold the last build's sorted codes
+// and permutation (when root->perm_valid).  The stable sort of the new codes by
+// (code, triangle) is unique, so if the last permutation orders them (non-decreasing
+// codes, equal codes by increasing triangle), it is that sort: keys1 takes the new
+// codes in that order and the radix passes have nothing to do.  If no code changed,
+// the de-duplicated leaves are the last build's too.
+__global__ void __launch_bounds__(BUILD_THREADS)
+k_coherence(const uint32_t* __restrict__ codes, uint32_t* keys1, const uint32_t* __restrict__ vals1, int nt,
+            const BvhRoot* __restrict__ root, uint32_t* mode) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t bad = 0;
+    if (!root->perm_valid) {
+        bad = M_UNSORTED | M_CHANGED;
+    } else if (i < nt) {
+        const uint32_t p = vals1[i];
+        if (p >= (uint32_t)nt) {
+            bad = M_UNSORTED | M_CHANGED;
+        } else {
+            const uint32_t c = codes[p];
+            if (c != keys1[i]) bad |= M_CHANGED;
+            if (i > 0) {
+                const uint32_t q = vals1[i - 1];
+                const uint32_t cq = q < (uint32_t)nt ? codes[q] : 0xffffffffu;
+                if (q >= (uint32_t)nt || cq > c || (cq == c && q > p)) bad |= M_UNSORTED;
+            }
+            keys1[i] = c;  // only this thread reads or writes entry i
+        }
+    }
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && bad) atomicOr(mode, bad);
+    if (i == 0) atomicOr(mode, M_RAN);
+}
+
 // One stable LSD pass over 8-bit digit (key >> shift) & 255.  Tiles are claimed in
 // launch order through an atomic counter, so every tile a block waits on belongs to a
 // block that is already running: the look-back always terminates.
 __global__ void __launch_bounds__(SORT_THREADS)
 k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
             uint32_t* __restrict__ vout, int n, int shift, const uint32_t* __restrict__ ghist,
-            uint32_t* status, uint32_t* counter, int* err) {
+            uint32_t* status, uint32_t* counter, const uint32_t* __restrict__ mode, int* err) {
+    if (skip_sort(*mode)) return;  // the last build's order stands
     __shared__ uint32_t s_whist[SORT_THREADS / 32][RADIX + 1];
     __shared__ uint32_t s_tstart[RADIX];
     __shared__ uint32_t s_gbase[RADIX];
@@ -307,7 +351,9 @@ k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, 
 // keep the first (lowest triangle index) of every run of equal codes
 __global__ void __launch_bounds__(SORT_THREADS)
 k_unique(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int n, uint32_t* __restrict__ ucode,
-         uint32_t* __restrict__ utri, uint32_t* status, uint32_t* counter, int n_tiles, BvhRoot* root, int* err) {
+         uint32_t* __restrict__ utri, uint32_t* status, uint32_t* counter, int n_tiles, BvhRoot* root,
+         const uint32_t* __restrict__ mode, int* err) {
+    if (skip_unique(*mode)) return;  // same codes: the last build's leaves stand
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_excl;
     __shared__ int s_tile;
@@ -356,7 +402,10 @@ k_unique(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, i
             st_volatile(st, ST_PREFIX | ((excl + tsum) & ST_VALUE));
         }
         s_excl = excl;
-        if (tile == n_tiles - 1) root->n_leaves = (int)min(excl + tsum, (uint32_t)n);
+        if (tile == n_tiles - 1) {
+            root->n_leaves = (int)min(excl + tsum, (uint32_t)n);
+            root->perm_valid = 1;  // k_build withdraws it if a wait of this build gave up
+        }
     }
     __syncthreads();
     uint32_t o = s_excl + incl - cnt;
@@ -414,6 +463,7 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
     const int nt = root->n_tris;
     const int n = min(root->n_leaves, nt);
     const int c0 = blockIdx.x * BUILD_LEAVES;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (*err & ERR_TIMEOUT)) root->perm_valid = 0;
     const int c1 = min(c0 + BUILD_LEAVES, n);
     s_flag[threadIdx.x] = 0u;
     __syncthreads();
@@ -572,7 +622,8 @@ void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
     a.want(&range, (size_t)ni);
     a.want(&root, 1);
     // histograms | sort status (PASSES x tiles x RADIX) | sort counters | unique status | unique counter
-    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 1;
+    // | rebuild mode word
+    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 2;
     a.want(&scratch, scratch_words);
 }
 
@@ -585,23 +636,27 @@ cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_e
     uint32_t* scount = sstat + (size_t)PASSES * b.tiles_sort * RADIX;
     uint32_t* ustat = scount + PASSES;
     uint32_t* ucount = ustat + b.tiles_sort;
+    uint32_t* mode = ucount + 1;
     k_body_prep<<<cdiv(b.nv, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.xyz_in, b.has_normals ? b.nrm_in : nullptr,
                                                                      b.nv, thickness, b.verts, b.root, b.nt);
     k_tri_boxes<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.verts, b.tris, b.nt, box_depth, b.tri_box,
                                                                      b.tri_leaf, b.root);
     k_morton<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.tri_box, b.nt, b.root, b.codes, ghist);
+    if (b.coherent)
+        k_coherence<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.codes, b.keys[1], b.vals[1], b.nt, b.root,
+                                                                         mode);
     const uint32_t* kin = b.codes;
     const uint32_t* vin = nullptr;
     for (int p = 0; p < PASSES; ++p) {
         uint32_t* ko = b.keys[p & 1];
         uint32_t* vo = b.vals[p & 1];
         k_sort_pass<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, ko, vo, b.nt, 8 * p, ghist + p * RADIX,
-                                                          sstat + (size_t)p * b.tiles_sort * RADIX, scount + p, d_err);
+                                                          sstat + (size_t)p * b.tiles_sort * RADIX, scount + p, mode, d_err);
         kin = ko;
         vin = vo;
     }
     k_unique<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, b.nt, b.ucode, b.utri, ustat, ucount, b.tiles_sort,
-                                                   b.root, d_err);
+                                                   b.root, mode, d_err);
     k_build<<<cdiv(b.nt, BUILD_LEAVES), BUILD_LEAVES, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes,
                                                                 b.leaves, b.flags, b.range, b.root, d_err);
     return cudaGetLastError();

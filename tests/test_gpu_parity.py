@@ -80,6 +80,47 @@ def test_lbvh_rebuild_after_update_matches_oracle():
         assert lbvh_diff(g.export_lbvh(), o.export_lbvh()) == []
 
 
+def line_soup(n=300):
+    """n tiny triangles along x, one per Morton cell (3.4 cells apart), same y and z."""
+    x = np.arange(n, dtype=np.float64) / n
+    v = np.zeros((n, 3, 3))
+    v[:, :, 0] = x[:, None]
+    v[:, 1, 0] += 1e-4
+    v[:, 2, 1] = 1e-4
+    return v.reshape(-1, 3).astype(np.float32), np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+
+
+def test_lbvh_coherent_rebuilds_match_oracle():
+    """A body rebuilt in place reuses the last build's sorted order while it still
+    sorts the new codes, and its leaves while no code changed: every outcome of that
+    check must give the tree a fresh build gives."""
+    xyz, tris = line_soup()
+    g, o = lbvh_pair(xyz, tris)
+    tri = xyz.reshape(-1, 3, 3)
+    steps = []
+    steps.append(tri.copy())                      # identical codes
+    t = tri.copy(); t[150, :, 0] += 1.0 / 1024    # one code changes, the order holds
+    steps.append(t)
+    t = tri.copy(); t[150] = tri[151]             # a new duplicate code: fewer leaves
+    steps.append(t)
+    t = tri.copy(); t[10], t[20] = tri[20], tri[10]  # order broken
+    steps.append(t)
+    steps.append(tri.copy())                      # back
+    steps.append(tri.copy())                      # identical again
+    rng = np.random.default_rng(4)
+    t = tri + rng.normal(0, 2e-3, tri.shape)      # many codes move
+    steps.append(t.astype(np.float32))
+    n_leaves = []
+    for t in steps:
+        p = np.ascontiguousarray(t, np.float32).reshape(-1, 3)
+        g.update_body(p, None)
+        o.update_body(p, None)
+        a, r = g.export_lbvh(), o.export_lbvh()
+        assert lbvh_diff(a, r) == []
+        n_leaves.append(a["n_leaves"])
+    assert n_leaves[0] == 300 and n_leaves[2] == 299 and n_leaves[4] == 300
+
+
 @pytest.mark.parametrize("name", ["ico3_noise", "capsules"])
 def test_first_hit_queries_match_oracle(name):
     b = BODIES[name]()
