@@ -111,8 +111,19 @@ struct BvhBuffers {
     uint32_t* utri = nullptr;    // T'
     Node* nodes = nullptr;       // nt-1
     float4* leaves = nullptr;    // 2*nt
-    uint32_t* flags = nullptr;   // nt-1 handshake counters (self-resetting)
     int2* range = nullptr;       // nt-1 leaf range of each internal node
+    // Summaries of the 512-leaf chunks for the nodes whose leaf range spans chunks
+    // (levels: per chunk, per 32 chunks, per 1024, per 32768, at lev_off[0..3])
+    int* cmin = nullptr;         // min delta over the boundaries of the entry's chunks
+    float4* cbox = nullptr;      // 2 per entry: union of the entry's leaf boxes
+    int2* srec = nullptr;        // 32 per chunk: suffix-minimum boundaries {position, delta}, right to left
+    float4* sbox = nullptr;      // 2 per record: union of the chunk's leaves after the boundary
+    int2* prec = nullptr;        // 32 per chunk: prefix-minimum boundaries, left to right
+    float4* pbox = nullptr;      // 2 per record: union of the chunk's leaves up to the boundary
+    int* rcnt = nullptr;         // 2 per chunk: suffix and prefix record counts
+    int2* top = nullptr;         // 64 per chunk: {boundary, delta} of the nodes that span chunks
+    int chunks = 0;              // chunks of nt leaves
+    int lev_off[4] = {0, 0, 0, 0};
     BvhRoot* root = nullptr;
     uint32_t* scratch = nullptr; // zeroed before every build (histograms, status words)
     size_t scratch_words = 0;

@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "visg_internal.cuh"
 
 namespace visg {
@@ -425,14 +427,6 @@ __device__ __forceinline__ int delta_at(const uint32_t* c, int i, int j, int n) 
     return (j < 0 || j >= n) ? -1 : __clz((int)(c[i] ^ c[j]));
 }
 
-// release/acquire add on a global counter (orders this thread's node writes before
-// the add, and the sibling's writes before this thread's later reads)
-__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
-    uint32_t old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-    return old;
-}
-
 // identity box (min +100, max -100) expanded by child A then child B
 __device__ __forceinline__ void merge_ab(float4 alo, float4 ahi, float4 blo, float4 bhi, float4& lo, float4& hi) {
     lo = make_float4(fminf(fminf(100.0f, alo.x), blo.x), fminf(fminf(100.0f, alo.y), blo.y),
@@ -441,37 +435,126 @@ __device__ __forceinline__ void merge_ab(float4 alo, float4 ahi, float4 blo, flo
                      fmaxf(fmaxf(-100.0f, ahi.z), bhi.z), 0.0f);
 }
 
-// Bottom-up build in two phases.  Each CTA owns the BUILD_LEAVES sorted leaves
-// [c0, c1).  Phase 1 climbs through the nodes split inside the chunk
-// (c0 <= g <= c1 - 2) with the handshake in shared memory: each child leaves its
-// box, link and far range end in its side of the node's slot; the first to arrive
-// stops, the second merges and climbs on.  A node whose other child lies in another
-// chunk never sees a second local arrival.  After one CTA barrier, phase 2 resumes
-// each such climb (and every climb that reached a node split outside the chunk)
-// with the handshake in global memory through acquire/release atomics.  Every node
-// still gets both child boxes (and its leaf range) written into global memory, in
-// the same A-then-B merge order, so the tree and the boxes are those of a single
-// global climb.
-constexpr int BUILD_LEAVES = 512;
+// The child (lo, hi, link) over leaves [l, r] enters its parent g: its side of the
+// node and of the node's leaf range.  hi.w carries delta at the boundary beyond the
+// child's far end (l - 1 for child A, r for child B).
+__device__ __forceinline__ void write_side(Node* nodes, int2* range, int g, bool is_a, float4 lo, float4 hi, int link,
+                                           int l, int r, int dfar) {
+    if (is_a) {
+        nodes[g].a_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+        nodes[g].a_hi = make_float4(hi.x, hi.y, hi.z, __int_as_float(dfar));
+        range[g].x = l;  // leaf ranges of the nodes (read by the export)
+    } else {
+        nodes[g].b_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+        nodes[g].b_hi = make_float4(hi.x, hi.y, hi.z, __int_as_float(dfar));
+        range[g].y = r;
+    }
+}
+
+// box union (fminf / fmaxf: exact, so any grouping gives the same box)
+__device__ __forceinline__ void box_union(float4& lo, float4& hi, float4 lo2, float4 hi2) {
+    lo = make_float4(fminf(lo.x, lo2.x), fminf(lo.y, lo2.y), fminf(lo.z, lo2.z), 0.0f);
+    hi = make_float4(fmaxf(hi.x, hi2.x), fmaxf(hi.y, hi2.y), fmaxf(hi.z, hi2.z), 0.0f);
+}
+__device__ __forceinline__ float4 ident_lo() { return make_float4(100.0f, 100.0f, 100.0f, 0.0f); }
+__device__ __forceinline__ float4 ident_hi() { return make_float4(-100.0f, -100.0f, -100.0f, 0.0f); }
+__device__ __forceinline__ float4 shfl_f4(float4 v, int o, bool up) {
+    return up ? make_float4(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o),
+                            __shfl_up_sync(0xffffffffu, v.z, o), 0.0f)
+              : make_float4(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o),
+                            __shfl_down_sync(0xffffffffu, v.z, o), 0.0f);
+}
+__device__ __forceinline__ void warp_box_reduce(float4& lo, float4& hi) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float4 l2 = make_float4(__shfl_xor_sync(0xffffffffu, lo.x, o), __shfl_xor_sync(0xffffffffu, lo.y, o),
+                                      __shfl_xor_sync(0xffffffffu, lo.z, o), 0.0f);
+        const float4 h2 = make_float4(__shfl_xor_sync(0xffffffffu, hi.x, o), __shfl_xor_sync(0xffffffffu, hi.y, o),
+                                      __shfl_xor_sync(0xffffffffu, hi.z, o), 0.0f);
+        box_union(lo, hi, l2, h2);
+    }
+}
+
+constexpr int BUILD_LEAVES = 512;  // leaves per chunk (one CTA, one leaf per thread)
+
+// Device view of the chunk summaries (see BvhBuffers).
+struct ChunkView {
+    int* cmin;
+    float4* cbox;
+    int2* srec;
+    float4* sbox;
+    int2* prec;
+    float4* pbox;
+    int* rcnt;
+    int2* top;
+    uint32_t* top_count;
+    uint32_t* done;
+    int lev_off[4];
+};
+constexpr int NLEV = 4;
+constexpr int BIG_DELTA = 64;  // above every delta: a boundary that does not exist
+
+// entries of each level for n leaves
+__device__ __forceinline__ void level_counts(int n, int cnt[NLEV]) {
+    cnt[0] = (n + BUILD_LEAVES - 1) / BUILD_LEAVES;
+#pragma unroll
+    for (int v = 1; v < NLEV; ++v) cnt[v] = (cnt[v - 1] + 31) / 32;
+}
+
+// Bottom-up build of the chunk-local nodes, and the chunk summaries.  Each CTA owns
+// the BUILD_LEAVES sorted leaves [c0, c1) and stages delta of the boundaries
+// c0 - 1 .. c1 - 1.  Phase 1 climbs through the nodes split inside the chunk
+// (c0 <= g <= c1 - 2) in shared memory only: each child leaves its box, link and far
+// range end in its side of the node's slot; the first to arrive stops, the second
+// merges (A then B) and climbs on.  After the barrier the nodes both of whose
+// children arrived are written out; a climb that stopped at a node whose other child
+// lies in another chunk, or at a node split outside the chunk, writes its side into
+// that node.  The remaining nodes span chunks; k_build_top finishes them from the
+// chunk summaries written here:
+//   * the boundaries that can end such a node's range inside this chunk: the strict
+//     suffix minima of delta (the nearest smaller delta to the left of a node
+//     further right) and the strict prefix minima (to the right of a node further
+//     left), at most 30 each, with the union of the chunk's leaf boxes beyond /
+//     up to each of them;
+//   * the chunk's min delta and leaf box union (and, from the last CTA to finish,
+//     the same per 32, 1024 and 32768 chunks);
+//   * the nodes of the chunk that span chunks (no smaller delta on one side inside
+//     the chunk, and the boundary to the next chunk).
 __global__ void __launch_bounds__(BUILD_LEAVES)
 k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, const float4* __restrict__ tri_box,
-        const float4* __restrict__ tri_leaf, Node* nodes, float4* __restrict__ leaves, uint32_t* flags, int2* range,
-        BvhRoot* root, int* err) {
-    __shared__ uint32_t s_flag[BUILD_LEAVES];
+        const float4* __restrict__ tri_leaf, Node* nodes, float4* __restrict__ leaves, int2* range, BvhRoot* root,
+        ChunkView cv, int* err) {
+    __shared__ uint32_t s_flag[BUILD_LEAVES];  // bit 0: child A arrived, bit 1: child B
     // per node and side (A, B): lo (w = link), hi (w = far range end)
     __shared__ float4 s_lo[BUILD_LEAVES][2], s_hi[BUILD_LEAVES][2];
+    __shared__ int s_delta[BUILD_LEAVES + 1];  // delta of boundary j at j - c0 + 1
+    constexpr int W = BUILD_LEAVES / 32;
+    __shared__ int s_wmin[W], s_wsr[W], s_wpr[W], s_wtop[W];
+    __shared__ float4 s_wlo[W], s_whi[W];
+    __shared__ uint32_t s_topbase;
+    __shared__ int s_last;
+    const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nt = root->n_tris;
     const int n = min(root->n_leaves, nt);
     const int c0 = blockIdx.x * BUILD_LEAVES;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && (*err & ERR_TIMEOUT)) root->perm_valid = 0;
     const int c1 = min(c0 + BUILD_LEAVES, n);
-    s_flag[threadIdx.x] = 0u;
+    const int chunk = (int)blockIdx.x;
+    if (blockIdx.x == 0 && tid == 0 && (*err & ERR_TIMEOUT)) root->perm_valid = 0;
+    s_flag[tid] = 0u;
+    {
+        const int j = c0 + tid;
+        s_delta[tid + 1] = delta_at(ucode, j, j + 1, n);  // -1 beyond the last leaf
+        if (tid == 0) s_delta[0] = c0 < n ? delta_at(ucode, c0, c0 - 1, n) : -1;
+    }
     __syncthreads();
-    const int i = c0 + (int)threadIdx.x;
+    const int i = c0 + tid;
     int l = i, r = i, link = ~i;  // the current subtree: leaf range, link
-    float4 lo = make_float4(0.0f, 0.0f, 0.0f, 0.0f), hi = lo;
+    float4 lo = ident_lo(), hi = ident_hi();
     bool live = i < n;  // still climbing
     int pend = -1;      // node where phase 1 stopped as the first local arrival
+    int out = -1;       // node split outside the chunk where phase 1 stopped
+    int dl = -1, dr = -1;
+    bool is_a = false;
     if (live) {
         const uint32_t t = min(utri[i], (uint32_t)(nt - 1));
         leaves[2 * i] = tri_leaf[2 * t];
@@ -485,35 +568,27 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             live = false;
         }
     }
-    // phase 1: handshakes in shared memory for nodes split inside the chunk
+    const float4 leaf_lo = lo, leaf_hi = hi;  // identity box for threads past the last leaf
     int level = 0;
     while (live) {
         if (++level > 64) {  // a climb is at most 31 levels over distinct 30-bit codes
             atomicOr(err, ERR_TIMEOUT);
-            live = false;
             break;
         }
-        const int dl = delta_at(ucode, l, l - 1, n);
-        const int dr = delta_at(ucode, r, r + 1, n);
-        const bool is_a = dr > dl;  // the parent extends to the right: this node is child A
+        dl = s_delta[l - c0];      // boundary l - 1
+        dr = s_delta[r - c0 + 1];  // boundary r
+        is_a = dr > dl;            // the parent extends to the right: this node is child A
         const int g = is_a ? r : l - 1;
-        if (g < c0 || g > c1 - 2) break;  // split outside the chunk: phase 2
-        if (is_a) {
-            nodes[g].a_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
-            nodes[g].a_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
-            range[g].x = l;  // leaf ranges of the nodes (read by the export)
-        } else {
-            nodes[g].b_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
-            nodes[g].b_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
-            range[g].y = r;
+        if (g < c0 || g > c1 - 2) {  // split outside the chunk
+            out = g;
+            break;
         }
         const int k = g - c0, side = is_a ? 0 : 1;
         s_lo[k][side] = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
         s_hi[k][side] = make_float4(hi.x, hi.y, hi.z, __int_as_float(is_a ? l : r));
         __threadfence_block();
-        if (atomicAdd(&s_flag[k], 1u) == 0u) {  // first to arrive: the sibling may be in another chunk
+        if (atomicOr(&s_flag[k], 1u << side) == 0u) {  // first to arrive: the sibling may be in another chunk
             pend = g;
-            live = false;
             break;
         }
         __threadfence_block();
@@ -532,63 +607,294 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             root->root = g;
             root->top_lo = lo;
             root->top_hi = hi;
-            live = false;
             break;
         }
     }
     __syncthreads();
-    // a climb that stopped first at a node whose other child never arrived locally
-    // resumes there: that child is in another chunk
-    bool resume = false;
-    if (pend >= 0 && s_flag[pend - c0] == 1u) {
-        live = true;
-        resume = true;
-        level = 0;
-    }
-    // phase 2: global handshakes.  A resumed climb re-enters at `pend` (its box and
-    // range are already in the node); the others continue from their current subtree.
-    while (live) {
-        if (++level > 64) {
-            atomicOr(err, ERR_TIMEOUT);
-            return;
+    // nodes of the chunk whose children both arrived here
+    {
+        const int g = c0 + tid;
+        if (g <= c1 - 2 && s_flag[tid] == 3u) {
+            const float4 alo = s_lo[tid][0], ahi = s_hi[tid][0], blo = s_lo[tid][1], bhi = s_hi[tid][1];
+            const int la = __float_as_int(ahi.w), rb = __float_as_int(bhi.w);
+            nodes[g].a_lo = alo;
+            nodes[g].a_hi = make_float4(ahi.x, ahi.y, ahi.z, __int_as_float(s_delta[la - c0]));
+            nodes[g].b_lo = blo;
+            nodes[g].b_hi = make_float4(bhi.x, bhi.y, bhi.z, __int_as_float(s_delta[rb - c0 + 1]));
+            range[g] = make_int2(la, rb);
         }
-        int g;
-        if (resume) {
-            g = pend;
-            resume = false;
-        } else {
-            const int dl = delta_at(ucode, l, l - 1, n);
-            const int dr = delta_at(ucode, r, r + 1, n);
-            const bool is_a = dr > dl;
-            g = is_a ? r : l - 1;
-            if (is_a) {
-                nodes[g].a_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
-                nodes[g].a_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
-                range[g].x = l;
-            } else {
-                nodes[g].b_lo = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
-                nodes[g].b_hi = make_float4(hi.x, hi.y, hi.z, 0.0f);
-                range[g].y = r;
+    }
+    // a climb that stopped at a node another chunk completes: its side, in the node
+    {
+        int g = out;
+        if (g < 0 && pend >= 0 && s_flag[pend - c0] != 3u) g = pend;
+        if (g >= 0) write_side(nodes, range, g, is_a, lo, hi, link, l, r, is_a ? dl : dr);
+    }
+    if (c0 < n) {
+        // thread tid: boundary j = c0 + tid (delta dk, BIG_DELTA past the last boundary)
+        // and leaf c0 + tid (its box, the identity box past the last leaf)
+        const int j = c0 + tid;
+        const int dk = j <= n - 2 ? s_delta[tid + 1] : BIG_DELTA;
+        int pm = dk, sm = dk;  // inclusive prefix / suffix min over the warp
+        float4 plo = leaf_lo, phi = leaf_hi, slo = leaf_lo, shi = leaf_hi;  // inclusive prefix / suffix unions
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int a = __shfl_up_sync(0xffffffffu, pm, o), b = __shfl_down_sync(0xffffffffu, sm, o);
+            const float4 al = shfl_f4(plo, o, true), ah = shfl_f4(phi, o, true);
+            const float4 bl = shfl_f4(slo, o, false), bh = shfl_f4(shi, o, false);
+            if (lane >= o) {
+                pm = min(pm, a);
+                box_union(plo, phi, al, ah);
+            }
+            if (lane + o < 32) {
+                sm = min(sm, b);
+                box_union(slo, shi, bl, bh);
             }
         }
-        if (atomic_add_acq_rel(&flags[g], 1u) == 0u) return;  // first child to arrive stops
-        flags[g] = 0u;  // both children seen: ready for the next build
-        const int2 rg = __ldcg(&range[g]);
-        l = rg.x;
-        r = rg.y;
-        if (l < 0 || r >= n || l > r) {
-            atomicOr(err, ERR_TIMEOUT);
-            return;
+        if (lane == 31) {
+            s_wmin[warp] = pm;
+            s_wlo[warp] = plo;
+            s_whi[warp] = phi;
         }
-        const float4 alo = __ldcg(&nodes[g].a_lo), ahi = __ldcg(&nodes[g].a_hi);
-        const float4 blo = __ldcg(&nodes[g].b_lo), bhi = __ldcg(&nodes[g].b_hi);
-        merge_ab(alo, ahi, blo, bhi, lo, hi);
-        link = g;
-        if (l == 0 && r == n - 1) {
-            root->root = g;
-            root->top_lo = lo;
-            root->top_hi = hi;
-            return;
+        __syncthreads();
+        // exclusive prefix / suffix over the other warps
+        int wpm = BIG_DELTA, wsm = BIG_DELTA;
+        float4 wplo = ident_lo(), wphi = ident_hi(), wslo = ident_lo(), wshi = ident_hi();
+        for (int w = 0; w < W; ++w) {
+            if (w < warp) {
+                wpm = min(wpm, s_wmin[w]);
+                box_union(wplo, wphi, s_wlo[w], s_whi[w]);
+            } else if (w > warp) {
+                wsm = min(wsm, s_wmin[w]);
+                box_union(wslo, wshi, s_wlo[w], s_whi[w]);
+            }
+        }
+        // strict prefix (suffix) minimum: delta below every delta to its left (right)
+        // in the chunk
+        const int ppm = __shfl_up_sync(0xffffffffu, pm, 1), nsm = __shfl_down_sync(0xffffffffu, sm, 1);
+        const int epm = min(wpm, lane > 0 ? ppm : BIG_DELTA);
+        const int esm = min(wsm, lane < 31 ? nsm : BIG_DELTA);
+        const bool pre = dk < epm, suf = dk < esm;
+        // the chunk's leaves up to leaf j, and after it
+        float4 up_lo = wplo, up_hi = wphi;
+        box_union(up_lo, up_hi, plo, phi);
+        float4 af_lo = wslo, af_hi = wshi;
+        {
+            const float4 nl = shfl_f4(slo, 1, false), nh = shfl_f4(shi, 1, false);
+            if (lane < 31) box_union(af_lo, af_hi, nl, nh);
+        }
+        // node of boundary j spans chunks: no smaller delta on one side inside the chunk,
+        // or j is the boundary to the next chunk
+        const bool span = j <= n - 2 && (j == c1 - 1 || (s_flag[tid] != 3u));
+        const unsigned bs = __ballot_sync(0xffffffffu, suf), bp = __ballot_sync(0xffffffffu, pre);
+        const unsigned bt = __ballot_sync(0xffffffffu, span);
+        if (lane == 0) {
+            s_wsr[warp] = __popc(bs);
+            s_wpr[warp] = __popc(bp);
+            s_wtop[warp] = __popc(bt);
+        }
+        __syncthreads();
+        int os = __popc(bs & ~((2u << lane) - 1u)), op = __popc(bp & ((1u << lane) - 1u));
+        int ot = __popc(bt & ((1u << lane) - 1u));
+        int ns = 0, np = 0, ntop = 0;
+        for (int w = 0; w < W; ++w) {
+            if (w > warp) os += s_wsr[w];
+            if (w < warp) {
+                op += s_wpr[w];
+                ot += s_wtop[w];
+            }
+            ns += s_wsr[w];
+            np += s_wpr[w];
+            ntop += s_wtop[w];
+        }
+        if (tid == 0) s_topbase = atomicAdd(cv.top_count, (uint32_t)ntop);
+        if (suf && os < 32) {
+            cv.srec[32 * chunk + os] = make_int2(j, dk);
+            cv.sbox[2 * (32 * chunk + os)] = af_lo;
+            cv.sbox[2 * (32 * chunk + os) + 1] = af_hi;
+        }
+        if (pre && op < 32) {
+            cv.prec[32 * chunk + op] = make_int2(j, dk);
+            cv.pbox[2 * (32 * chunk + op)] = up_lo;
+            cv.pbox[2 * (32 * chunk + op) + 1] = up_hi;
+        }
+        if (tid == BUILD_LEAVES - 1) {  // holds the whole chunk's prefix
+            cv.rcnt[2 * chunk] = min(ns, 32);
+            cv.rcnt[2 * chunk + 1] = min(np, 32);
+            cv.cmin[chunk] = min(wpm, pm);
+            cv.cbox[2 * chunk] = up_lo;
+            cv.cbox[2 * chunk + 1] = up_hi;
+        }
+        __syncthreads();
+        if (span) {
+            const uint32_t pos = s_topbase + (uint32_t)ot;
+            if (pos < (uint32_t)(64 * gridDim.x)) cv.top[pos] = make_int2(j, dk);
+        }
+    }
+    // the last CTA to finish sums the chunks up per 32, 1024 and 32768 chunks
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(cv.done, 1u) == gridDim.x - 1u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    int cnt[NLEV];
+    level_counts(n, cnt);
+    for (int v = 1; v < NLEV; ++v) {
+        const int* mi = cv.cmin + cv.lev_off[v - 1];
+        const float4* bi = cv.cbox + 2 * cv.lev_off[v - 1];
+        for (int e = warp; e < cnt[v]; e += W) {
+            const int k = 32 * e + lane;
+            int m = BIG_DELTA;
+            float4 blo = ident_lo(), bhi = ident_hi();
+            if (k < cnt[v - 1]) {
+                m = __ldcg(mi + k);
+                blo = __ldcg(bi + 2 * k);
+                bhi = __ldcg(bi + 2 * k + 1);
+            }
+            warp_box_reduce(blo, bhi);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (lane == 0) {
+                cv.cmin[cv.lev_off[v] + e] = m;
+                cv.cbox[2 * (cv.lev_off[v] + e)] = blo;
+                cv.cbox[2 * (cv.lev_off[v] + e) + 1] = bhi;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Nearest entry of level 0 (a chunk) left of chunk c (right, with right) whose min
+// delta is below d, through the summary levels: scan the 32 entries of the current
+// group, climb a level while nothing qualifies, then descend into the first group
+// that does.  -1: none.
+__device__ int nearest_chunk(const ChunkView& cv, const int cnt[NLEV], int c, int d, bool right, int lane, int* err) {
+    int idx = c;
+    for (int v = 0; v < NLEV; ++v) {
+        const int* m = cv.cmin + cv.lev_off[v];
+        const int base = idx & ~31, e = base + lane;
+        const bool hit = (right ? e > idx : e < idx) && e < cnt[v] && __ldg(m + e) < d;
+        unsigned b = __ballot_sync(0xffffffffu, hit);
+        if (b) {
+            int f = right ? base + __ffs(b) - 1 : base + 31 - __clz(b);
+            for (int u = v - 1; u >= 0; --u) {  // descend: the first qualifying entry of group f
+                const int b2 = 32 * f, e2 = b2 + lane;
+                const bool h2 = e2 < cnt[u] && __ldg(cv.cmin + cv.lev_off[u] + e2) < d;
+                b = __ballot_sync(0xffffffffu, h2);
+                if (!b) {  // the group's min said otherwise: corrupt summaries
+                    if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+                    return -1;
+                }
+                f = right ? b2 + __ffs(b) - 1 : b2 + 31 - __clz(b);
+            }
+            return f;
+        }
+        if (right ? base + 32 >= cnt[v] : base == 0) return -1;  // no group beyond this one
+        idx >>= 5;
+    }
+    return -1;
+}
+
+// First record (in the records' order) of chunk c with delta below d whose position is
+// left of g (right of g, with right); g < 0: any position.  -1: none.
+__device__ __forceinline__ int first_record(const int2* rec, int count, int g, int d, bool right, int lane,
+                                            int2& out) {
+    const int2 q = lane < count ? __ldg(rec + lane) : make_int2(0, BIG_DELTA);
+    const bool hit = lane < count && q.y < d && (g < 0 || (right ? q.x > g : q.x < g));
+    const unsigned b = __ballot_sync(0xffffffffu, hit);
+    if (!b) return -1;
+    const int k = __ffs(b) - 1;
+    out = make_int2(__shfl_sync(0xffffffffu, q.x, k), __shfl_sync(0xffffffffu, q.y, k));
+    return k;
+}
+
+// union of the leaf boxes of chunks [a, b] (warp-uniform a, b), in every lane
+__device__ void chunk_union(const ChunkView& cv, const int cnt[NLEV], int a, int b, int lane, float4& lo,
+                            float4& hi) {
+    float4 ul = ident_lo(), uh = ident_hi();
+    for (int v = 0; v < NLEV && a <= b; ++v) {
+        const float4* bx = cv.cbox + 2 * cv.lev_off[v];
+        if ((a >> 5) == (b >> 5) || v == NLEV - 1) {
+            for (int e = a + lane; e <= b; e += 32) box_union(ul, uh, __ldg(bx + 2 * e), __ldg(bx + 2 * e + 1));
+            break;
+        }
+        const int e1 = a + lane, e2 = (b & ~31) + lane;
+        if (e1 <= (a | 31)) box_union(ul, uh, __ldg(bx + 2 * e1), __ldg(bx + 2 * e1 + 1));
+        if (e2 <= b) box_union(ul, uh, __ldg(bx + 2 * e2), __ldg(bx + 2 * e2 + 1));
+        a = (a >> 5) + 1;
+        b = (b >> 5) - 1;
+    }
+    warp_box_reduce(ul, uh);
+    box_union(lo, hi, ul, uh);
+}
+
+// The nodes whose leaf range spans chunks, one warp each, independently: the range
+// ends are the nearest boundaries with a smaller delta on either side (the first
+// suffix / prefix record past the node with a smaller delta, in the node's chunk or
+// in the nearest chunk with a smaller min), the box is the union of the leaf boxes in
+// the range (the records' partial unions and whole chunks between), and the node
+// enters its parent (the range end with the larger delta) as build_internal's climb
+// would have put it there.
+constexpr int TOP_WARPS = 8;
+__global__ void __launch_bounds__(TOP_WARPS * 32)
+k_build_top(ChunkView cv, Node* nodes, int2* range, BvhRoot* root, int* err) {
+    const int nt = root->n_tris;
+    const int n = min(root->n_leaves, nt);
+    int cnt[NLEV];
+    level_counts(n, cnt);
+    const int lane = (int)(threadIdx.x & 31u);
+    const uint32_t count = min(*cv.top_count, (uint32_t)(64 * cnt[0]));
+    const uint32_t nw = gridDim.x * TOP_WARPS;
+    for (uint32_t it = blockIdx.x * TOP_WARPS + (threadIdx.x >> 5); it < count; it += nw) {
+        const int2 item = __ldg(cv.top + it);
+        const int g = item.x, d = item.y, c = g / BUILD_LEAVES;
+        if (g < 0 || g > n - 2 || c >= cnt[0]) {
+            if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+            continue;
+        }
+        // left end: boundary jl (leaves from jl + 1), -1 = none
+        int2 q;
+        int jl = -1, dlft = -1, cl = -1;
+        float4 lo = ident_lo(), hi = ident_hi();
+        int k = first_record(cv.srec + 32 * c, __ldg(cv.rcnt + 2 * c), g, d, false, lane, q);
+        int cc = c;
+        if (k < 0) {
+            cc = nearest_chunk(cv, cnt, c, d, false, lane, err);
+            if (cc >= 0) k = first_record(cv.srec + 32 * cc, __ldg(cv.rcnt + 2 * cc), -1, d, false, lane, q);
+        }
+        if (k >= 0) {
+            jl = q.x;
+            dlft = q.y;
+            cl = cc;
+            box_union(lo, hi, __ldg(cv.sbox + 2 * (32 * cc + k)), __ldg(cv.sbox + 2 * (32 * cc + k) + 1));
+        }
+        // right end: boundary jr (leaves up to jr), n - 1 = none
+        int jr = n - 1, drgt = -1, cr = cnt[0] - 1;
+        k = first_record(cv.prec + 32 * c, __ldg(cv.rcnt + 2 * c + 1), g, d, true, lane, q);
+        cc = c;
+        if (k < 0) {
+            cc = nearest_chunk(cv, cnt, c, d, true, lane, err);
+            if (cc >= 0) k = first_record(cv.prec + 32 * cc, __ldg(cv.rcnt + 2 * cc + 1), -1, d, true, lane, q);
+        }
+        if (k >= 0) {
+            jr = q.x;
+            drgt = q.y;
+            cr = cc;
+            box_union(lo, hi, __ldg(cv.pbox + 2 * (32 * cc + k)), __ldg(cv.pbox + 2 * (32 * cc + k) + 1));
+        } else {
+            box_union(lo, hi, __ldg(cv.cbox + 2 * cr), __ldg(cv.cbox + 2 * cr + 1));  // the last chunk
+        }
+        chunk_union(cv, cnt, cl + 1, cr - 1, lane, lo, hi);
+        if (lane == 0) {
+            if (jl < 0 && jr == n - 1) {
+                root->root = g;
+                root->top_lo = lo;
+                root->top_hi = hi;
+            } else {
+                const bool is_a = drgt > dlft;
+                write_side(nodes, range, is_a ? jr : jl, is_a, lo, hi, g, jl + 1, jr, is_a ? dlft : drgt);
+            }
         }
     }
 }
@@ -618,12 +924,26 @@ void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
     a.want(&utri, (size_t)nt + 1);
     a.want(&nodes, (size_t)ni);
     a.want(&leaves, (size_t)nt * 2 + 2);
-    a.want(&flags, (size_t)ni);
     a.want(&range, (size_t)ni);
+    chunks = cdiv(std::max(nt, 1), BUILD_LEAVES);
+    int entries = 0, e = chunks;
+    for (int v = 0; v < NLEV; ++v) {
+        lev_off[v] = entries;
+        entries += e;
+        e = cdiv(e, 32);
+    }
+    a.want(&cmin, (size_t)entries);
+    a.want(&cbox, 2 * (size_t)entries);
+    a.want(&srec, 32 * (size_t)chunks);
+    a.want(&sbox, 64 * (size_t)chunks);
+    a.want(&prec, 32 * (size_t)chunks);
+    a.want(&pbox, 64 * (size_t)chunks);
+    a.want(&rcnt, 2 * (size_t)chunks);
+    a.want(&top, 64 * (size_t)chunks);
     a.want(&root, 1);
     // histograms | sort status (PASSES x tiles x RADIX) | sort counters | unique status | unique counter
-    // | rebuild mode word
-    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 2;
+    // | rebuild mode word | top list count | finished chunk CTAs
+    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 4;
     a.want(&scratch, scratch_words);
 }
 
@@ -637,6 +957,8 @@ cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_e
     uint32_t* ustat = scount + PASSES;
     uint32_t* ucount = ustat + b.tiles_sort;
     uint32_t* mode = ucount + 1;
+    ChunkView cv{b.cmin, b.cbox, b.srec, b.sbox, b.prec, b.pbox, b.rcnt, b.top, mode + 1, mode + 2,
+                 {b.lev_off[0], b.lev_off[1], b.lev_off[2], b.lev_off[3]}};
     k_body_prep<<<cdiv(b.nv, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.xyz_in, b.has_normals ? b.nrm_in : nullptr,
                                                                      b.nv, thickness, b.verts, b.root, b.nt);
     k_tri_boxes<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.verts, b.tris, b.nt, box_depth, b.tri_box,
@@ -657,8 +979,11 @@ cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_e
     }
     k_unique<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, b.nt, b.ucode, b.utri, ustat, ucount, b.tiles_sort,
                                                    b.root, mode, d_err);
-    k_build<<<cdiv(b.nt, BUILD_LEAVES), BUILD_LEAVES, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes,
-                                                                b.leaves, b.flags, b.range, b.root, d_err);
+    k_build<<<b.chunks, BUILD_LEAVES, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes, b.leaves, b.range,
+                                               b.root, cv, d_err);
+    if (b.chunks > 1)  // else the whole tree is one chunk's
+        k_build_top<<<std::min(cdiv(64 * b.chunks, TOP_WARPS), 1024), TOP_WARPS * 32, 0, s>>>(cv, b.nodes, b.range,
+                                                                                              b.root, d_err);
     return cudaGetLastError();
 }
 

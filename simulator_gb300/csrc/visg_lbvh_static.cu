@@ -7,7 +7,7 @@
 // footprint after initialisation.  visg_lbvh_build_noalloc serves them: the caller
 // passes the body (device pointers) and the output arrays, and every temporary the
 // build needs (boxes, Morton codes, radix-sort buffers, look-back status words,
-// handshake flags) lives in one file-scope __device__ array, so the call itself
+// chunk summaries) lives in one file-scope __device__ array, so the call itself
 // allocates nothing.
 //
 // Costs and limits:
@@ -125,10 +125,9 @@ extern "C" int visg_lbvh_build_noalloc(const float* d_xyz, const float* d_normal
     b.ucode = d_sorted_codes;
     b.utri = reinterpret_cast<uint32_t*>(d_sorted_tris);
 
-    // what must start at zero: the error word and the handshake flags (the build
-    // clears its histograms and look-back status words itself)
+    // what must start at zero: the error word (the build clears its histograms,
+    // look-back status words and counters itself)
     cudaError_t e = cudaMemsetAsync(d_err, 0, 4, s);
-    if (e == cudaSuccess && n_tris > 1) e = cudaMemsetAsync(b.flags, 0, (size_t)(n_tris - 1) * 4, s);
     if (e == cudaSuccess) e = lbvh_build(b, thickness, box_depth, d_err, s);
     if (e == cudaSuccess && n_tris > 1) {
         const unsigned grid = (unsigned)((n_tris + 255) / 256);
