@@ -63,6 +63,44 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
 }
 __device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *reinterpret_cast<volatile uint32_t*>(p) = v; }
 
+// Decoupled look-back: the exclusive prefix of tile `tile` from the status words of
+// the tiles before it (tile t's at st0[t * stride]: 0 = not yet published, ST_AGG |
+// its own count, ST_PREFIX | its inclusive prefix).  A word only ever goes from 0 to
+// AGG to PREFIX, so one read of it stays valid: LB_WINDOW predecessors are read per
+// round trip, summed in order down to the first PREFIX; a word still 0 is waited on
+// (bounded) and the walk resumes there.
+constexpr int LB_WINDOW = 8;
+__device__ __forceinline__ uint32_t look_back(const uint32_t* st0, size_t stride, int tile, int* err) {
+    uint32_t excl = 0;
+    int t = tile - 1, spins = 0;
+    while (t >= 0) {
+        uint32_t w[LB_WINDOW];
+#pragma unroll
+        for (int q = 0; q < LB_WINDOW; ++q) w[q] = t - q >= 0 ? ld_volatile(st0 + (size_t)(t - q) * stride) : 0u;
+        int q = 0;
+        bool done = false;
+        for (; q < LB_WINDOW && t - q >= 0; ++q) {
+            const uint32_t f = w[q] & ~ST_VALUE;
+            if (f == 0u) break;  // not published yet
+            excl += w[q] & ST_VALUE;
+            if (f == ST_PREFIX) {
+                done = true;
+                break;
+            }
+        }
+        if (done) break;
+        t -= q;
+        if (q < LB_WINDOW) {  // stopped at an unpublished tile (tile 0 always publishes a PREFIX)
+            if (++spins > SPIN_LIMIT) {
+                atomicOr(err, ERR_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    return excl;
+}
+
 // inclusive scan of one value per thread over a 256-thread block
 __device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* s_warp) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -308,23 +346,7 @@ k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, 
         st_volatile(st, ST_PREFIX | tcount);
     } else {
         st_volatile(st, ST_AGG | tcount);
-        int t = tile - 1;
-        int spins = 0;
-        while (t >= 0) {
-            uint32_t s = ld_volatile(status + (size_t)t * RADIX + d);
-            uint32_t f = s & ~ST_VALUE;
-            if (f == 0u) {
-                if (++spins > SPIN_LIMIT) {
-                    atomicOr(err, ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(32);
-                continue;
-            }
-            excl += s & ST_VALUE;
-            if (f == ST_PREFIX) break;
-            --t;
-        }
+        excl = look_back(status + d, RADIX, tile, err);
         st_volatile(st, ST_PREFIX | ((excl + tcount) & ST_VALUE));
     }
     s_gbase[d] = goff + excl;
@@ -385,22 +407,7 @@ k_unique(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, i
             st_volatile(st, ST_PREFIX | tsum);
         } else {
             st_volatile(st, ST_AGG | tsum);
-            int t = tile - 1, spins = 0;
-            while (t >= 0) {
-                uint32_t s = ld_volatile(status + t);
-                uint32_t f = s & ~ST_VALUE;
-                if (f == 0u) {
-                    if (++spins > SPIN_LIMIT) {
-                        atomicOr(err, ERR_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
-                }
-                excl += s & ST_VALUE;
-                if (f == ST_PREFIX) break;
-                --t;
-            }
+            excl = look_back(status, 1, tile, err);
             st_volatile(st, ST_PREFIX | ((excl + tsum) & ST_VALUE));
         }
         s_excl = excl;
@@ -529,8 +536,12 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
     __shared__ float4 s_lo[BUILD_LEAVES][2], s_hi[BUILD_LEAVES][2];
     __shared__ int s_delta[BUILD_LEAVES + 1];  // delta of boundary j at j - c0 + 1
     constexpr int W = BUILD_LEAVES / 32;
-    __shared__ int s_wmin[W], s_wsr[W], s_wpr[W], s_wtop[W];
+    __shared__ int s_wmin[W], s_wsr[W], s_wpr[W], s_wtop[W];  // per warp
     __shared__ float4 s_wlo[W], s_whi[W];
+    // per warp, over the warps before (x*p) / after (x*s) it
+    __shared__ int s_xpm[W], s_xsm[W], s_xos[W], s_xop[W], s_xot[W];
+    __shared__ float4 s_xplo[W], s_xphi[W], s_xslo[W], s_xshi[W];
+    __shared__ int s_nrec[2];
     __shared__ uint32_t s_topbase;
     __shared__ int s_last;
     const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -555,10 +566,9 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
     int out = -1;       // node split outside the chunk where phase 1 stopped
     int dl = -1, dr = -1;
     bool is_a = false;
+    uint32_t t = 0;  // the leaf's triangle
     if (live) {
-        const uint32_t t = min(utri[i], (uint32_t)(nt - 1));
-        leaves[2 * i] = tri_leaf[2 * t];
-        leaves[2 * i + 1] = tri_leaf[2 * t + 1];
+        t = min(utri[i], (uint32_t)(nt - 1));
         lo = tri_box[2 * t];
         hi = tri_box[2 * t + 1];
         if (n == 1) {
@@ -611,6 +621,10 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
         }
     }
     __syncthreads();
+    if (i < n) {  // after the climbs: no global store is pending at their fences
+        leaves[2 * i] = tri_leaf[2 * t];
+        leaves[2 * i + 1] = tri_leaf[2 * t + 1];
+    }
     // nodes of the chunk whose children both arrived here
     {
         const int g = c0 + tid;
@@ -657,18 +671,27 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             s_whi[warp] = phi;
         }
         __syncthreads();
-        // exclusive prefix / suffix over the other warps
-        int wpm = BIG_DELTA, wsm = BIG_DELTA;
-        float4 wplo = ident_lo(), wphi = ident_hi(), wslo = ident_lo(), wshi = ident_hi();
-        for (int w = 0; w < W; ++w) {
-            if (w < warp) {
-                wpm = min(wpm, s_wmin[w]);
-                box_union(wplo, wphi, s_wlo[w], s_whi[w]);
-            } else if (w > warp) {
-                wsm = min(wsm, s_wmin[w]);
-                box_union(wslo, wshi, s_wlo[w], s_whi[w]);
+        if (tid < W) {  // exclusive prefix / suffix over the warps, for warp tid
+            int a = BIG_DELTA, b = BIG_DELTA;
+            float4 al = ident_lo(), ah = ident_hi(), bl = ident_lo(), bh = ident_hi();
+            for (int w = 0; w < W; ++w) {
+                if (w < tid) {
+                    a = min(a, s_wmin[w]);
+                    box_union(al, ah, s_wlo[w], s_whi[w]);
+                } else if (w > tid) {
+                    b = min(b, s_wmin[w]);
+                    box_union(bl, bh, s_wlo[w], s_whi[w]);
+                }
             }
+            s_xpm[tid] = a;
+            s_xsm[tid] = b;
+            s_xplo[tid] = al;
+            s_xphi[tid] = ah;
+            s_xslo[tid] = bl;
+            s_xshi[tid] = bh;
         }
+        __syncthreads();
+        const int wpm = s_xpm[warp], wsm = s_xsm[warp];
         // strict prefix (suffix) minimum: delta below every delta to its left (right)
         // in the chunk
         const int ppm = __shfl_up_sync(0xffffffffu, pm, 1), nsm = __shfl_down_sync(0xffffffffu, sm, 1);
@@ -676,9 +699,9 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
         const int esm = min(wsm, lane < 31 ? nsm : BIG_DELTA);
         const bool pre = dk < epm, suf = dk < esm;
         // the chunk's leaves up to leaf j, and after it
-        float4 up_lo = wplo, up_hi = wphi;
+        float4 up_lo = s_xplo[warp], up_hi = s_xphi[warp];
         box_union(up_lo, up_hi, plo, phi);
-        float4 af_lo = wslo, af_hi = wshi;
+        float4 af_lo = s_xslo[warp], af_hi = s_xshi[warp];
         {
             const float4 nl = shfl_f4(slo, 1, false), nh = shfl_f4(shi, 1, false);
             if (lane < 31) box_union(af_lo, af_hi, nl, nh);
@@ -694,20 +717,31 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             s_wtop[warp] = __popc(bt);
         }
         __syncthreads();
-        int os = __popc(bs & ~((2u << lane) - 1u)), op = __popc(bp & ((1u << lane) - 1u));
-        int ot = __popc(bt & ((1u << lane) - 1u));
-        int ns = 0, np = 0, ntop = 0;
-        for (int w = 0; w < W; ++w) {
-            if (w > warp) os += s_wsr[w];
-            if (w < warp) {
-                op += s_wpr[w];
-                ot += s_wtop[w];
+        if (tid < W) {
+            int xs = 0, xp = 0, xt = 0, ts = 0, tp = 0, tt = 0;
+            for (int w = 0; w < W; ++w) {
+                if (w > tid) xs += s_wsr[w];
+                if (w < tid) {
+                    xp += s_wpr[w];
+                    xt += s_wtop[w];
+                }
+                ts += s_wsr[w];
+                tp += s_wpr[w];
+                tt += s_wtop[w];
             }
-            ns += s_wsr[w];
-            np += s_wpr[w];
-            ntop += s_wtop[w];
+            s_xos[tid] = xs;
+            s_xop[tid] = xp;
+            s_xot[tid] = xt;
+            if (tid == 0) {
+                s_nrec[0] = ts;
+                s_nrec[1] = tp;
+                s_topbase = atomicAdd(cv.top_count, (uint32_t)tt);
+            }
         }
-        if (tid == 0) s_topbase = atomicAdd(cv.top_count, (uint32_t)ntop);
+        __syncthreads();
+        const int os = __popc(bs & ~((2u << lane) - 1u)) + s_xos[warp];
+        const int op = __popc(bp & ((1u << lane) - 1u)) + s_xop[warp];
+        const int ot = __popc(bt & ((1u << lane) - 1u)) + s_xot[warp];
         if (suf && os < 32) {
             cv.srec[32 * chunk + os] = make_int2(j, dk);
             cv.sbox[2 * (32 * chunk + os)] = af_lo;
@@ -719,13 +753,12 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             cv.pbox[2 * (32 * chunk + op) + 1] = up_hi;
         }
         if (tid == BUILD_LEAVES - 1) {  // holds the whole chunk's prefix
-            cv.rcnt[2 * chunk] = min(ns, 32);
-            cv.rcnt[2 * chunk + 1] = min(np, 32);
+            cv.rcnt[2 * chunk] = min(s_nrec[0], 32);
+            cv.rcnt[2 * chunk + 1] = min(s_nrec[1], 32);
             cv.cmin[chunk] = min(wpm, pm);
             cv.cbox[2 * chunk] = up_lo;
             cv.cbox[2 * chunk + 1] = up_hi;
         }
-        __syncthreads();
         if (span) {
             const uint32_t pos = s_topbase + (uint32_t)ot;
             if (pos < (uint32_t)(64 * gridDim.x)) cv.top[pos] = make_int2(j, dk);
