@@ -17,7 +17,9 @@ Reported (one JSON line, rank 0):
   e2e         the same through the C ABI with host buffers: every step uploads the
               pinned-vertex targets from pinned host memory, steps, and reads all
               positions back into pinned host memory (the read of step k overlaps
-              step k + 1; the timed region ends when the last read has landed)
+              step k + 1; the timed region ends when the last read has landed),
+              with the host link's own device-to-host rate for the same bytes
+              (its ceiling: every step moves all positions over the link)
   plain_loop  the same garments as 256 plain simulators stepped one after another
   roofline    the fused step kernel: algorithmic bytes per launch / launch time
   cpu_baseline the CPU restatement (OpenMP) on the same garments, bounded sample
@@ -373,6 +375,22 @@ def main():
     e2e_value = world * nv * k_e2e / e2e_s
     h2d = len(pins) * (4 + 12)
     d2h = nv * 12
+    # the host link's own device-to-host rate for the same bytes (plain copies into
+    # the same page-locked buffer): the end-to-end loop's ceiling
+    src = torch.empty(nv * 3, dtype=torch.float32, device="cuda")
+    dst = torch.from_numpy(outs[0].reshape(-1))
+    for _ in range(2):
+        dst.copy_(src, non_blocking=True)
+    torch.cuda.synchronize()
+    l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0.record()
+    for _ in range(10):
+        dst.copy_(src, non_blocking=True)
+    l1.record()
+    torch.cuda.synchronize()
+    link_gbs = 10 * d2h / (l0.elapsed_time(l1) / 1e3) / 1e9
+    del src
+    d2h_gbs = d2h * k_e2e / e2e_s / 1e9
 
     # ---- the plain per-garment loop on the same GPU ------------------------------------
     plain = None
@@ -429,7 +447,8 @@ def main():
                        "l2": f"inputs larger than L2: {alg_bytes / 1e6:.0f} MB moved per step vs 129 MB L2",
                        "parallelism": f"{world} independent batches (one per GPU)"},
             "e2e": {"value": e2e_value, "unit": "vertex-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": k_e2e},
+                    "d2h_bytes_per_step": d2h, "steps": k_e2e, "d2h_gbs": d2h_gbs,
+                    "link_d2h_gbs_measured": link_gbs, "frac_of_link": d2h_gbs / link_gbs},
             "plain_loop": plain,
             "batched_vs_plain": (value / plain["value"]) if plain else None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -27,7 +27,7 @@
 //           shared memory; count 0 = read from global memory
 //   per body: LBVH nodes (64 B: both children's boxes and links), leaves (32 B:
 //           v0 and the face normal), root record; build scratch (sort buffers,
-//           look-back status words, handshake flags)
+//           look-back status words, chunk summaries)
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

@@ -18,15 +18,20 @@
 //                 (ties keep triangle order, i.e. sort by (code, triangle))
 //   k_unique      keep the first triangle of every distinct code
 //                 (remove_redundant, Utilities.h:35-55), look-back compaction
-//   k_build       bottom-up radix-tree build fused with the refit: each leaf thread
-//                 climbs (handshakes in shared memory while both children lie in the
-//                 CTA's chunk of leaves, in global memory above), the parent of range [l, r] is the boundary with the longer
-//                 common prefix (delta(l-1,l) vs delta(r,r+1), delta = clz(a ^ b) as
-//                 cudaBRT.cu:9-19), the second child to arrive merges both boxes into
-//                 the identity box (calculateBoudingBox, cudaBRT.cu:166-206) and
-//                 continues.  Nodes are numbered by their split position; the tree is
-//                 the same binary radix tree processInternalNode (cudaBRT.cu:120-161)
-//                 builds, and visg_export_lbvh renumbers it into the reference's layout.
+//   k_build       bottom-up radix-tree build fused with the refit, per chunk of 512
+//                 sorted leaves: each leaf thread climbs with handshakes in shared
+//                 memory while both children lie in the chunk; the parent of range
+//                 [l, r] is the boundary with the longer common prefix (delta(l-1,l)
+//                 vs delta(r,r+1), delta = clz(a ^ b) as cudaBRT.cu:9-19), the second
+//                 child to arrive merges both boxes into the identity box
+//                 (calculateBoudingBox, cudaBRT.cu:166-206) and continues.  Each chunk
+//                 then publishes a summary for the nodes that span chunks
+//   k_build_top   one warp per node that spans chunks: its range ends are the nearest
+//                 boundaries with a smaller delta, its box the union of its leaves'
+//                 boxes, both read off the chunk summaries
+//                 Nodes are numbered by their split position; the tree is the same
+//                 binary radix tree processInternalNode (cudaBRT.cu:120-161) builds,
+//                 and visg_export_lbvh renumbers it into the reference's layout.
 // Every wait is bounded; a wait that gives up sets ERR_TIMEOUT and the host reports
 // VISG_ERR_TIMEOUT.
 #include <cuda_runtime.h>
