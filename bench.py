@@ -203,25 +203,28 @@ def cpu_baseline(items, params, seconds: float, states=None, settle: int = 0):
                       f"({el:.1f} s), {threads} OpenMP threads"}
 
 
-def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: int):
-    """The plain single-garment workloads whose body moves (LBVH rebuilt every step):
-    per step the body's positions (precomputed on the device) go in through
-    update_body_device, then one step runs.  Also times the same steps with the
-    body held still, so the rebuild's share shows."""
+def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: int, substeps: int = 4):
+    """The plain single-garment workloads whose body moves (LBVH rebuilt every step),
+    each over its stated duration (1,000 frames for the capsules, 500 for the sphere,
+    `substeps` steps per frame), from the initial state: the sheet falls, meets the
+    moving body and drapes over it.  Per step the body's positions (precomputed on the
+    device) go in through update_body_device, then one step runs.  Then `steps` more
+    steps with the body held still show the rebuild's share."""
     out = {}
-    for name, make in (("garment_over_capsules", scenes.garment_over_capsules),
-                       ("sheet_over_noisy_sphere", scenes.sheet_over_noisy_sphere)):
+    for name, make, frames in (("garment_over_capsules", scenes.garment_over_capsules, 1000),
+                               ("sheet_over_noisy_sphere", scenes.sheet_over_noisy_sphere, 500)):
         cloth, body, motion = make(0)
         n = len(cloth.xyz)
         sim = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
                            pinned=cloth.pinned)
         sim.set_stream(stream.cuda_stream)
-        total = warmup + 2 * steps
-        base = body.xyz.astype(np.float64)
-        frames = np.stack([(base + motion(k * params.dt)).astype(np.float32) for k in range(total)])
-        d_frames = torch.from_numpy(frames).cuda()
+        timed = frames * substeps
+        total = warmup + timed
+        offs = np.stack([motion(k * params.dt) for k in range(total)]).astype(np.float32)
+        d_base = torch.from_numpy(np.ascontiguousarray(body.xyz, np.float32)).cuda()
+        d_frames = (d_base[None] + torch.from_numpy(offs).cuda()[:, None, :]).contiguous()
         d_nrm = torch.from_numpy(np.ascontiguousarray(body.normals, np.float32)).cuda()
-        fb = d_frames.element_size() * base.size
+        fb = d_frames.element_size() * d_base.numel()
 
         def run(k0, k, move):
             for j in range(k0, k0 + k):
@@ -233,19 +236,22 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
         torch.cuda.synchronize()
         e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         e[0].record(stream)
-        run(warmup, steps, True)
+        run(warmup, timed, True)
         e[1].record(stream)
+        torch.cuda.synchronize()
+        contacts = sim.count_contacts()
         e[2].record(stream)
-        run(warmup + steps, steps, False)
+        run(0, steps, False)
         e[3].record(stream)
         torch.cuda.synchronize()
-        ms_move = e[0].elapsed_time(e[1]) / steps
+        ms_move = e[0].elapsed_time(e[1]) / timed
         ms_still = e[2].elapsed_time(e[3]) / steps
         out[name] = {"vertices": n, "spring_entries": int(sum(sl.n_entries for sl in cloth.lists)),
-                     "triangles": int(len(body.tris)), "steps": steps,
+                     "triangles": int(len(body.tris)), "frames": frames, "steps": timed,
                      "value": n / (ms_move / 1e3), "unit": "vertex-steps/s", "ms_per_step": ms_move,
                      "ms_per_step_body_still": ms_still, "lbvh_rebuild_ms": ms_move - ms_still,
-                     "contacts": sim.count_contacts()}
+                     "contacts_at_end": contacts}
+        del d_frames
         sim.close()
     return out
 
@@ -306,7 +312,8 @@ def main():
 
     params = scenes.physics_params(args.substeps)
     if args.moving_only:
-        out = moving_body_configs(vs, scenes, torch, params, torch.cuda.current_stream(), args.steps, args.warmup)
+        out = moving_body_configs(vs, scenes, torch, params, torch.cuda.current_stream(), args.steps, args.warmup,
+                                  args.substeps)
         print(json.dumps({"moving_body_configs": out}), flush=True)
         return 0
     if args.stage is not None:
@@ -418,11 +425,11 @@ def main():
             s.close()
     moving = None
     if rank == 0 and not args.no_moving:
-        moving = moving_body_configs(vs, scenes, torch, params, stream, 100, 10)
+        moving = moving_body_configs(vs, scenes, torch, params, stream, 100, 10, args.substeps)
     clocks = sampler.stop()
 
     # ---- roofline of the fused step kernel ---------------------------------------------
-    # SURVEY 8(d) per-unit figure B_int = 72 N + 4 (N+1) L + s E with one merged row
+    # the per-unit figure B_int = 72 N + 4 (N+1) L + s E with one merged row
     # list (L = 1) and 8-byte entries (s = 8): x, x_old, normal read and written as
     # 12-byte vectors, the row offset, and one entry per directed spring
     alg_bytes = 72 * nv + 4 * (nv + 1) + 8 * ne

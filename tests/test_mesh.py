@@ -13,10 +13,11 @@ import numpy as np
 import pytest
 
 import simulator_gb300 as vs
+from oracle.build import REFERENCE
 from simulator_gb300 import scenes
 
 F = np.float32
-REF_RES = "/root/reference/resources"
+REF_RES = os.path.join(REFERENCE, "resources")  # the reference tree the oracle's recipe builds from
 
 
 def test_obj_reader_forms(tmp_path):
