@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--settle", type=int, default=2400, help="untimed steps before the warm-up (draping)")
     ap.add_argument("--cpu-garments", type=int, default=16, help="garments in the CPU baseline's sample")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="weak: every rank its own batch (seed + rank); strong: one batch sharded by vertex count")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-garment loop")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-moving", action="store_true", help="skip the moving-body plain configs")
@@ -289,22 +291,11 @@ def main():
     import simulator_gb300 as vs
     from simulator_gb300 import scenes
 
+    from simulator_gb300.shards import RankGroup, my_shard
+
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    group = RankGroup("nccl", device=torch.device("cuda", local))
+    barrier, max_over_ranks = group.barrier, group.max
 
     vis = os.environ.get("CUDA_VISIBLE_DEVICES")
     phys = int(vis.split(",")[local]) if vis and vis.split(",")[local].strip().isdigit() else local
@@ -318,7 +309,16 @@ def main():
         return 0
     if args.stage is not None:
         params.stage_neighbours = args.stage
-    items, nv, ne, nt = build_workload(args.garments, args.seed + rank)
+    if args.scaling == "strong":  # one batch, sharded by vertex count
+        items, _, _, _ = build_workload(args.garments, args.seed)
+        lo, hi = my_shard([len(c.xyz) for c, _ in items], rank, world)
+        items = items[lo:hi]
+        nv = sum(len(c.xyz) for c, _ in items)
+        ne = sum(sum(sl.n_entries for sl in c.lists) for c, _ in items)
+        nt = sum(len(b.tris) for _, b in items)
+    else:  # every rank its own batch
+        items, nv, ne, nt = build_workload(args.garments, args.seed + rank)
+    nv_all = group.sum(nv)  # vertices stepped by all ranks
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
 
@@ -353,7 +353,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     ms = max_over_ranks(e0.elapsed_time(e1))
-    value = world * nv * args.steps / (ms / 1e3)
+    value = nv_all * args.steps / (ms / 1e3)
     contacts = b.count_contacts()
 
     # ---- end to end through the C ABI with host buffers --------------------------------
@@ -379,7 +379,7 @@ def main():
             b.wait_positions()  # step k - 1's positions are in host memory
     b.wait_positions()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = world * nv * k_e2e / e2e_s
+    e2e_value = nv_all * k_e2e / e2e_s
     h2d = len(pins) * (4 + 12)
     d2h = nv * 12
     # the host link's own device-to-host rate for the same bytes (plain copies into
@@ -419,7 +419,7 @@ def main():
         p1.record(stream)
         torch.cuda.synchronize()
         pms = max_over_ranks(p0.elapsed_time(p1))
-        plain = {"value": world * nv * args.steps / (pms / 1e3), "ms_per_step": pms / args.steps,
+        plain = {"value": nv_all * args.steps / (pms / 1e3), "ms_per_step": pms / args.steps,
                  "how": "each garment its own Simulator, stepped K steps (graph replay) one garment after another"}
         for s in sims:
             s.close()
@@ -446,13 +446,15 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": args.scaling,
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": workload_name(args), "garments": args.garments, "vertices_per_gpu": nv,
+                       "vertices_all_gpus": int(nv_all),
                        "spring_entries": ne, "triangles": nt, "contacts": contacts,
                        "launch": launch,
                        "l2": f"inputs larger than L2: {alg_bytes / 1e6:.0f} MB moved per step vs 129 MB L2",
-                       "parallelism": f"{world} independent batches (one per GPU)"},
+                       "parallelism": (f"{world} independent batches (one per GPU)" if args.scaling == "weak"
+                                       else f"one batch in {world} shards by vertex count (one per GPU)")},
             "e2e": {"value": e2e_value, "unit": "vertex-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": k_e2e, "d2h_gbs": d2h_gbs,
                     "link_d2h_gbs_measured": link_gbs, "frac_of_link": d2h_gbs / link_gbs},
@@ -468,8 +470,7 @@ def main():
             "gpu_launches": args.steps * launch["kernels_per_step"],
         }
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    group.close()
     return 0
 
 
