@@ -74,6 +74,11 @@ typedef struct VisgParams {
                                 while it stays within it, redoing only the plane test
                                 (default); 0: query every step.  Same results;
                                 update_body clears the caches.                           */
+    int32_t overlap_groups;  /* batches: 0 (default) steps the garments as two groups of about
+                                equal vertex count, each its own chain of kernels on its own
+                                stream inside the step graphs, so one group's collision pass
+                                and kernel boundaries overlap the other's step; 1: one chain.
+                                Same results.                                             */
 } VisgParams;
 
 void visg_default_params(VisgParams* p);

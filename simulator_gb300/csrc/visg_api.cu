@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -106,6 +107,13 @@ struct Engine {
     VisgParams p{};
     cudaStream_t stream = nullptr;
     cudaStream_t cap = nullptr;
+    cudaStream_t cap2 = nullptr;  // the second group's capture stream
+    cudaStream_t run2 = nullptr;  // the second group's stream outside graphs
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, fork2 = nullptr, join2 = nullptr;
+    // garment groups stepped as independent chains: group 1 starts at garment
+    // boundary vsplit (vertex), i.e. at tile tsplit[b] of each tile table
+    int tsplit[3] = {0, 0, 0};
+    int64_t vsplit = 0;
     bool finalized = false;
     std::vector<GarmentIn> gin;
     int G = 0;
@@ -202,6 +210,10 @@ struct Engine {
         arena.release();
         if (h_status) cudaFreeHost(h_status);
         if (cap) cudaStreamDestroy(cap);
+        if (cap2) cudaStreamDestroy(cap2);
+        if (run2) cudaStreamDestroy(run2);
+        for (cudaEvent_t ev : {fork_ev, join_ev, fork2, join2})
+            if (ev) cudaEventDestroy(ev);
     }
 
     void destroy_graphs() {
@@ -283,6 +295,12 @@ struct Engine {
         CU(cudaGetDevice(&dev));
         CU(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
         CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        CU(cudaStreamCreateWithFlags(&cap2, cudaStreamNonBlocking));
+        CU(cudaStreamCreateWithFlags(&run2, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&fork2, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&join2, cudaEventDisableTiming));
         CU(cudaHostAlloc((void**)&h_status, 16, cudaHostAllocDefault));
         G = (int)gin.size();
         const int L = p.n_lists;
@@ -385,6 +403,17 @@ struct Engine {
                         twin[b].push_back(make_int2(0, 0));
                     }
                 }
+        }
+        // the two garment groups: split at the garment boundary nearest half the vertices
+        if (G >= 2) {
+            int gs = 1;
+            for (int g = 2; g < G; ++g)
+                if (std::llabs(2 * voff[g] - N) < std::llabs(2 * voff[gs] - N)) gs = g;
+            vsplit = voff[gs];
+            for (int b = 0; b < 3; ++b) {
+                tsplit[b] = 0;
+                while (tsplit[b] < (int)tiles[b].size() && tiles[b][tsplit[b]].x < gs) ++tsplit[b];
+            }
         }
         // plan the allocation
         arena.want(&d_state[0], 2 * (size_t)N + 2);
@@ -508,7 +537,10 @@ struct Engine {
         return sp;
     }
 
-    StepArgs args(int from, int blk) const {
+    // step chains per step: two garment groups, or one
+    int groups() const { return (G >= 2 && p.overlap_groups != 1) ? 2 : 1; }
+
+    StepArgs args(int from, int blk, int grp = 0) const {
         StepArgs a;
         a.state_in = d_state[from];
         a.state_out = d_state[from ^ 1];
@@ -517,36 +549,64 @@ struct Engine {
         a.ent = d_ent;
         a.kent = d_k;
         int bi = block_index(blk);
-        a.tiles = d_tiles[bi];
-        a.n_tiles = n_tiles[bi];
+        const int two = groups() == 2;
+        const int t0 = (two && grp == 1) ? tsplit[bi] : 0, t1 = (two && grp == 0) ? tsplit[bi] : n_tiles[bi];
+        a.tiles = d_tiles[bi] + t0;
+        a.n_tiles = t1 - t0;
         a.bodies = d_views;
         a.err = d_err;
         a.check = d_check;
-        a.cand = d_cand;
-        a.cand_count = d_cand_count;
+        a.cand = d_cand + ((two && grp == 1) ? vsplit : 0);  // a group queues at most its own vertices
+        a.cand_count = d_cand_count + ((two && grp == 1) ? 1 : 0);
         a.hitleaf = d_hitleaf;
         a.sell = d_sell;
         a.sellk = d_sellk;
         a.slice_off = d_slice_off;
         a.vcount = d_vcount;
         a.wild = d_wild;
-        a.twin = d_twin[bi];
+        a.twin = d_twin[bi] + t0;
         a.win_cap = win_cap[bi];
         a.p = step_params();
         return a;
     }
 
-    cudaError_t launch_one(cudaStream_t s, int from) { return launch_step(args(from, block), variant(block), block, grid, s); }
+    // one step; with two groups the second runs on its own stream (forked from and
+    // joined back to s) so the two chains overlap as they do in the step graphs
+    cudaError_t launch_one(cudaStream_t s, int from) {
+        if (groups() == 1) return launch_step(args(from, block, 0), variant(block), block, grid, s);
+        cudaError_t e = cudaEventRecord(fork2, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(run2, fork2, 0);
+        if (e == cudaSuccess) e = launch_step(args(from, block, 1), variant(block), block, grid, run2);
+        cudaError_t e0 = launch_step(args(from, block, 0), variant(block), block, grid, s);
+        cudaError_t ej = cudaEventRecord(join2, run2);
+        if (ej == cudaSuccess) ej = cudaStreamWaitEvent(s, join2, 0);
+        return e != cudaSuccess ? e : (e0 != cudaSuccess ? e0 : ej);
+    }
 
+    // chunk_steps steps as one graph; with two groups each group's steps form their own
+    // chain on its own capture stream (forked at the start, joined at the end), so
+    // the chains overlap when the graph runs
     int capture_chunk(int c) {
         cudaGraph_t g = nullptr;
+        const int ng = groups();
         CU(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        int from = c;
         cudaError_t le = cudaSuccess;
-        for (int k = 0; k < chunk_steps; ++k) {
-            cudaError_t e = launch_one(cap, from);
-            if (e != cudaSuccess && le == cudaSuccess) le = e;
+        if (ng == 2) {
+            le = cudaEventRecord(fork_ev, cap);
+            if (le == cudaSuccess) le = cudaStreamWaitEvent(cap2, fork_ev, 0);
+        }
+        int from = c;
+        for (int k = 0; k < chunk_steps && le == cudaSuccess; ++k) {
+            for (int gr = 0; gr < ng; ++gr) {
+                cudaError_t e = launch_step(args(from, block, gr), variant(block), block, grid, gr ? cap2 : cap);
+                if (e != cudaSuccess && le == cudaSuccess) le = e;
+            }
             from ^= 1;
+        }
+        if (ng == 2) {  // join, even after an error, so the capture can end
+            cudaError_t e = cudaEventRecord(join_ev, cap2);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(cap, join_ev, 0);
+            if (e != cudaSuccess && le == cudaSuccess) le = e;
         }
         cudaError_t ee = cudaStreamEndCapture(cap, &g);
         if (le != cudaSuccess) {
@@ -1179,6 +1239,7 @@ void visg_default_params(VisgParams* p) {
     p->split_collision = 1;
     p->stage_neighbours = 0;
     p->collision_margin = 1;
+    p->overlap_groups = 0;
 }
 
 const char* visg_version(void) { return "visg-gb300 1.0 (sm_103a)"; }
@@ -1470,7 +1531,7 @@ int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas, int32_t*
     if (ctas) *ctas = e.sm_count > 0 ? e.grid / e.sm_count : 0;
     if (split) *split = (v & SV_SPLIT) ? 1 : 0;
     if (stage) *stage = (v & SV_STAGED) ? 1 : 0;
-    if (kernels) *kernels = (v & SV_SPLIT) ? 2 : 1;
+    if (kernels) *kernels = ((v & SV_SPLIT) ? 2 : 1) * e.groups();
     return VISG_OK;
 }
 

@@ -31,6 +31,7 @@ class VisgParams(C.Structure):
         ("split_collision", C.c_int32),
         ("stage_neighbours", C.c_int32),
         ("collision_margin", C.c_int32),
+        ("overlap_groups", C.c_int32),
     ]
 
 
@@ -56,6 +57,7 @@ def reference_params(n_lists: int = 2) -> VisgParams:
     p.split_collision = 1
     p.stage_neighbours = 0
     p.collision_margin = 1
+    p.overlap_groups = 0
     return p
 
 
@@ -63,7 +65,7 @@ def make_params(n_lists: int, dt: float, mass: float, gravity=(0.0, -9.8, 0.0), 
                 spring_damping=0.0, verlet_damping=1.0, thickness=0.003, box_depth=0.01,
                 list_k=(100.0, 2.0, 2.0, 2.0), collide=1, check_every=0, max_displacement=1.0,
                 use_graph=1, split_collision=1, stage_neighbours=0,
-                collision_margin=1) -> VisgParams:
+                collision_margin=1, overlap_groups=0) -> VisgParams:
     p = VisgParams()
     p.dt, p.mass = dt, mass
     p.gravity[:] = tuple(gravity)
@@ -76,4 +78,5 @@ def make_params(n_lists: int, dt: float, mass: float, gravity=(0.0, -9.8, 0.0), 
     p.split_collision = split_collision
     p.stage_neighbours = stage_neighbours
     p.collision_margin = collision_margin
+    p.overlap_groups = overlap_groups
     return p

@@ -416,6 +416,32 @@ def test_batch_equals_plain_per_garment():
         assert np.array_equal(allx[b.offsets[gi]:b.offsets[gi + 1]], x)
 
 
+@pytest.mark.parametrize("stage", [0, 1])
+def test_batch_two_step_chains_equal_one(stage):
+    """The default batch steps its garments as two groups, each its own chain of
+    kernels on its own stream inside the step graphs; one chain gives the same
+    trajectory (the bench's physics: fast path, query cache, draping on spheres)."""
+    items = scenes.garment_batch(6, seed=3, side_range=(24, 72), subdiv_range=(2, 4), radius_range=(0.2, 0.25),
+                                 centre_depth=0.3)
+    out = []
+    for groups in (0, 1):
+        p = scenes.physics_params(4)
+        p.stage_neighbours = stage
+        p.overlap_groups = groups
+        b = vs.BatchSimulator(p)
+        for cloth, body in items:
+            b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+        b.finalize()
+        assert b.launch_info()["kernels_per_step"] == (4 if groups == 0 else 2)
+        b.step(16 * 40 + 7)  # graph chunks, then single steps
+        out.append((b.state(), b.count_contacts()))
+        b.close()
+    (a, ca), (c, cc) = out
+    assert ca == cc and ca > 0
+    for u, v in zip(a, c):
+        assert np.array_equal(u, v)
+
+
 def test_pipelined_position_reads_equal_synchronous_reads():
     cloth, cl, body, p = ref_scene(side=24, subdiv=2)
     a = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
