@@ -418,7 +418,7 @@ k_unique(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, i
         s_excl = excl;
         if (tile == n_tiles - 1) {
             root->n_leaves = (int)min(excl + tsum, (uint32_t)n);
-            root->perm_valid = 1;  // k_build withdraws it if a wait of this build gave up
+            root->perm_valid = 1;  // k_build withdraws it if a wait of this LBVH build gave up
         }
     }
     __syncthreads();
