@@ -99,12 +99,13 @@ def peak_hbm():
 
 
 def committed_traffic():
-    """Per-launch DRAM bytes of the fused step from the committed ncu summary."""
+    """DRAM bytes of the fused step kernel per step (all its launches) from the
+    committed ncu summary."""
     try:
         text = open(TRAFFIC_FILE).read()
     except OSError:
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    m = re.search(r"traffic_bytes_per_step:\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
