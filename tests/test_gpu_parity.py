@@ -58,6 +58,15 @@ def test_lbvh_soups_match_oracle(n, dup):
     assert lbvh_diff(g.export_lbvh(), o.export_lbvh()) == []
 
 
+def test_lbvh_million_triangle_soup_matches_oracle():
+    """About 1,950 chunks of 512 leaves: nodes spanning chunks are resolved through
+    the chunk summaries' second and third levels (per 32 and per 1,024 chunks)."""
+    xyz, tris = soup(1_000_000, seed=17, dup_frac=0.1)
+    g, o = lbvh_pair(xyz, tris)
+    a, r = g.export_lbvh(), o.export_lbvh()
+    assert a["n_leaves"] > 900_000 and lbvh_diff(a, r) == []
+
+
 def test_lbvh_single_distinct_code():
     one = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
     xyz = np.concatenate([one] * 7)
@@ -440,6 +449,37 @@ def test_batch_two_step_chains_equal_one(stage):
     assert ca == cc and ca > 0
     for u, v in zip(a, c):
         assert np.array_equal(u, v)
+
+
+def test_full_bench_batch_equals_plain_garments():
+    """Size-independent property at the bench's full size (256 garments, 6.8 M
+    vertices, draped on their spheres, the bench's launch shape): garments stepped
+    inside the batch follow the same trajectories, bit for bit, as plain single-garment
+    simulators started from the same state (whose parity with the oracle the smaller
+    tests establish)."""
+    items = scenes.garment_batch(256, seed=0)
+    p = scenes.physics_params(4)
+    p.stage_neighbours = 1
+    b = vs.BatchSimulator(p)
+    for cloth, body in items:
+        b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+    b.finalize()
+    b.set_launch(512, 2)
+    b.step(2400)
+    assert b.count_contacts() > 100_000
+    sizes = np.array([len(c.xyz) for c, _ in items])
+    pick = [int(sizes.argmin()), int(np.argsort(sizes)[len(sizes) // 2]), int(sizes.argmax())]
+    start = {gi: b.state(gi) for gi in pick}
+    b.step(40)
+    for gi in pick:
+        cloth, body = items[gi]
+        s = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=p, pinned=cloth.pinned)
+        s.set_state(*start[gi])
+        s.simulate(40)
+        for u, v in zip(b.state(gi), s.state()):
+            assert np.array_equal(u, v), gi
+        s.close()
+    b.close()
 
 
 def test_pipelined_position_reads_equal_synchronous_reads():
