@@ -23,6 +23,10 @@ Reported (one JSON line, rank 0):
   plain_loop  the same garments as 256 plain simulators stepped one after another
   roofline    the fused step kernel: algorithmic bytes per launch / launch time
   cpu_baseline the CPU restatement (OpenMP) on the same garments, bounded sample
+  moving_body_configs  the plain configurations whose body moves (LBVH rebuilt
+              every step), over their stated durations
+  adjoint_config  500 FP64 forward steps (checkpoint every 50) + the backward
+              sweep on a 128 x 128 sheet with a stiffness per spring
 `--impl reference` times the reference's step logic on the host cores (the
 oracle port; the reference itself is CUDA only) on the same workload.
 """
@@ -65,6 +69,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-garment loop")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-moving", action="store_true", help="skip the moving-body plain configs")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable (adjoint) config")
     ap.add_argument("--moving-only", action="store_true",
                     help="only the moving-body plain configs (one JSON object; for profiling the LBVH rebuild)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -259,6 +264,40 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
     return out
 
 
+def adjoint_config(vs, scenes, torch):
+    """The differentiable configuration: a 128 x 128 sheet (16,384 vertices) with a
+    stiffness per spring (the three lists' k as per-entry arrays) over the 64 x 64
+    workload's sphere (radius 0.3 m, subdivision 4, centre 0.5 m below), 500 FP64
+    forward steps with a checkpoint every 50, then the backward sweep (the gradient of
+    a mean squared final-position error for every spring's stiffness and the three
+    damping scalars).  Host wall-clock around each call (both synchronise)."""
+    cloth = scenes.grid_cloth(128, 1.0, 0.0)
+    body = scenes.icosphere(4, 0.3, center=(0.0, -0.5, 0.0))
+    p = scenes.physics_params(2)
+    lists = [scenes.SpringList(sl.row, sl.ent, np.full(sl.n_entries, k, np.float32))
+             for sl, k in zip(cloth.lists, (2000.0, 1000.0, 500.0))]
+    sim = vs.Simulator(cloth.xyz, lists, body.xyz, body.tris, body.normals, params=p, pinned=cloth.pinned)
+    steps, ckpt = 500, 50
+    sim.forward(steps, ckpt)  # warm: allocations, first launches
+    sim.backward(np.zeros_like(cloth.xyz))
+    sim.set_state(cloth.xyz, cloth.xyz, np.zeros_like(cloth.xyz))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.forward(steps, ckpt)
+    t1 = time.perf_counter()
+    x = sim.positions()
+    target = cloth.xyz + np.float32(0.005)
+    dk, ds = sim.backward((2.0 * (x - target) / len(x)).astype(np.float32))
+    t2 = time.perf_counter()
+    n = len(cloth.xyz)
+    out = {"vertices": n, "spring_entries": int(sum(sl.n_entries for sl in lists)), "steps": steps,
+           "checkpoint_every": ckpt, "forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+           "value": n * steps / (t2 - t0), "unit": "vertex-steps/s (forward + backward)",
+           "grad_max_abs": float(np.abs(dk).max()), "contacts": sim.count_contacts()}
+    sim.close()
+    return out
+
+
 # ---------------------------------------------------------------------------------------
 def run_reference(args, rank):
     if rank != 0:
@@ -427,6 +466,9 @@ def main():
     moving = None
     if rank == 0 and not args.no_moving:
         moving = moving_body_configs(vs, scenes, torch, params, stream, 100, 10, args.substeps)
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = adjoint_config(vs, scenes, torch)
     clocks = sampler.stop()
 
     # ---- roofline of the fused step kernel ---------------------------------------------
@@ -467,6 +509,7 @@ def main():
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "moving_body_configs": moving,
+            "adjoint_config": adjoint,
             "clocks": clocks,
             "gpu_launches": args.steps * launch["kernels_per_step"],
         }
