@@ -223,6 +223,7 @@ k_morton(const float4* __restrict__ tri_box, int nt, BvhRoot* root, uint32_t* __
         root->frame_lo = make_float4(s_frame[0], s_frame[1], s_frame[2], 0.0f);
         root->frame_hi = make_float4(s_frame[3], s_frame[4], s_frame[5], 0.0f);
     }
+    uint32_t code = 0u;
     if (t < nt) {
         float4 lo = tri_box[2 * t], hi = tri_box[2 * t + 1];
         f3 c = divs(add(xyz(lo), xyz(hi)), 2.0f);  // BBox::centroid
@@ -233,10 +234,22 @@ k_morton(const float4* __restrict__ tri_box, int nt, BvhRoot* root, uint32_t* __
         float x = fminf(fmaxf(__fmul_rn(q.x, 1024.0f), 0.0f), 1023.0f);
         float y = fminf(fmaxf(__fmul_rn(q.y, 1024.0f), 0.0f), 1023.0f);
         float z = fminf(fmaxf(__fmul_rn(q.z, 1024.0f), 0.0f), 1023.0f);
-        uint32_t code = expand_bits((uint32_t)x) * 4u + expand_bits((uint32_t)y) * 2u + expand_bits((uint32_t)z);
+        code = expand_bits((uint32_t)x) * 4u + expand_bits((uint32_t)y) * 2u + expand_bits((uint32_t)z);
         codes[t] = code;
+    }
+    // digit counts of the four radix passes; the two high digits are nearly constant
+    // across a block's neighbouring triangles, so their lanes add once per equal digit
+    const int lane = threadIdx.x & 31;
+    const bool ok = t < nt;
 #pragma unroll
-        for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p][(code >> (8 * p)) & 255u], 1u);
+    for (int p = 0; p < PASSES; ++p) {
+        const uint32_t dig = (code >> (8 * p)) & 255u;
+        if (p < 2) {
+            if (ok) atomicAdd(&s_hist[p][dig], 1u);
+        } else {
+            const uint32_t peers = __match_any_sync(0xffffffffu, ok ? dig : RADIX);
+            if (ok && lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][dig], (uint32_t)__popc(peers));
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) {
