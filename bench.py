@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--launch", default=None, help="block,ctas_per_sm instead of autotuning (profiling runs)")
     ap.add_argument("--stage", type=int, default=None, help="stage_neighbours with --launch (profiling runs)")
+    ap.add_argument("--chains", type=int, default=2, choices=[1, 2],
+                    help="step chains per step: 2 overlapping garment groups (default) or 1 (profiling runs)")
     return ap.parse_args()
 
 
@@ -349,6 +351,7 @@ def main():
         return 0
     if args.stage is not None:
         params.stage_neighbours = args.stage
+    params.overlap_groups = 0 if args.chains == 2 else 1
     if args.scaling == "strong":  # one batch, sharded by vertex count
         items, _, _, _ = build_workload(args.garments, args.seed)
         lo, hi = my_shard([len(c.xyz) for c, _ in items], rank, world)
