@@ -120,7 +120,7 @@ struct BvhBuffers {
     float4* sbox = nullptr;      // 2 per record: union of the chunk's leaves after the boundary
     int2* prec = nullptr;        // 32 per chunk: prefix-minimum boundaries, left to right
     float4* pbox = nullptr;      // 2 per record: union of the chunk's leaves up to the boundary
-    int* rcnt = nullptr;         // 2 per chunk: suffix and prefix record counts
+    int* rcnt = nullptr;         // 3 per chunk: suffix and prefix record counts, nodes in `top`
     int2* top = nullptr;         // 64 per chunk: {boundary, delta} of the nodes that span chunks
     int chunks = 0;              // chunks of nt leaves
     int lev_off[4] = {0, 0, 0, 0};

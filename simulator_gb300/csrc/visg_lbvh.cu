@@ -512,7 +512,6 @@ struct ChunkView {
     float4* pbox;
     int* rcnt;
     int2* top;
-    uint32_t* top_count;
     uint32_t* done;
     int lev_off[4];
 };
@@ -559,8 +558,7 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
     // per warp, over the warps before (x*p) / after (x*s) it
     __shared__ int s_xpm[W], s_xsm[W], s_xos[W], s_xop[W], s_xot[W];
     __shared__ float4 s_xplo[W], s_xphi[W], s_xslo[W], s_xshi[W];
-    __shared__ int s_nrec[2];
-    __shared__ uint32_t s_topbase;
+    __shared__ int s_nrec[3];
     __shared__ int s_last;
     const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nt = root->n_tris;
@@ -570,12 +568,6 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
     const int chunk = (int)blockIdx.x;
     if (blockIdx.x == 0 && tid == 0 && (*err & ERR_TIMEOUT)) root->perm_valid = 0;
     s_flag[tid] = 0u;
-    {
-        const int j = c0 + tid;
-        s_delta[tid + 1] = delta_at(ucode, j, j + 1, n);  // -1 beyond the last leaf
-        if (tid == 0) s_delta[0] = c0 < n ? delta_at(ucode, c0, c0 - 1, n) : -1;
-    }
-    __syncthreads();
     const int i = c0 + tid;
     int l = i, r = i, link = ~i;  // the current subtree: leaf range, link
     float4 lo = ident_lo(), hi = ident_hi();
@@ -584,17 +576,23 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
     int out = -1;       // node split outside the chunk where phase 1 stopped
     int dl = -1, dr = -1;
     bool is_a = false;
-    uint32_t t = 0;  // the leaf's triangle
+    uint32_t t = 0;  // the leaf's triangle (its box loads overlap the code loads below)
     if (live) {
         t = min(utri[i], (uint32_t)(nt - 1));
         lo = tri_box[2 * t];
         hi = tri_box[2 * t + 1];
-        if (n == 1) {
-            root->root = -1;
-            root->top_lo = lo;
-            root->top_hi = hi;
-            live = false;
-        }
+    }
+    {
+        const int j = c0 + tid;
+        s_delta[tid + 1] = delta_at(ucode, j, j + 1, n);  // -1 beyond the last leaf
+        if (tid == 0) s_delta[0] = c0 < n ? delta_at(ucode, c0, c0 - 1, n) : -1;
+    }
+    __syncthreads();
+    if (live && n == 1) {
+        root->root = -1;
+        root->top_lo = lo;
+        root->top_hi = hi;
+        live = false;
     }
     const float4 leaf_lo = lo, leaf_hi = hi;  // identity box for threads past the last leaf
     int level = 0;
@@ -753,7 +751,7 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             if (tid == 0) {
                 s_nrec[0] = ts;
                 s_nrec[1] = tp;
-                s_topbase = atomicAdd(cv.top_count, (uint32_t)tt);
+                s_nrec[2] = tt;
             }
         }
         __syncthreads();
@@ -771,16 +769,14 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             cv.pbox[2 * (32 * chunk + op) + 1] = up_hi;
         }
         if (tid == BUILD_LEAVES - 1) {  // holds the whole chunk's prefix
-            cv.rcnt[2 * chunk] = min(s_nrec[0], 32);
-            cv.rcnt[2 * chunk + 1] = min(s_nrec[1], 32);
+            cv.rcnt[3 * chunk] = min(s_nrec[0], 32);
+            cv.rcnt[3 * chunk + 1] = min(s_nrec[1], 32);
+            cv.rcnt[3 * chunk + 2] = min(s_nrec[2], 64);
             cv.cmin[chunk] = min(wpm, pm);
             cv.cbox[2 * chunk] = up_lo;
             cv.cbox[2 * chunk + 1] = up_hi;
         }
-        if (span) {
-            const uint32_t pos = s_topbase + (uint32_t)ot;
-            if (pos < (uint32_t)(64 * gridDim.x)) cv.top[pos] = make_int2(j, dk);
-        }
+        if (span && ot < 64) cv.top[64 * chunk + ot] = make_int2(j, dk);  // at most 61 per chunk
     }
     // the last CTA to finish sums the chunks up per 32, 1024 and 32768 chunks
     __threadfence();
@@ -895,10 +891,14 @@ k_build_top(ChunkView cv, Node* nodes, int2* range, BvhRoot* root, int* err) {
     int cnt[NLEV];
     level_counts(n, cnt);
     const int lane = (int)(threadIdx.x & 31u);
-    const uint32_t count = min(*cv.top_count, (uint32_t)(64 * cnt[0]));
+    // each chunk's nodes that span chunks sit in its 64 slots; iteration `it` takes slot
+    // it / F of chunk it % F, so the (few, low) occupied slots spread over all warps
+    const uint32_t F = (uint32_t)cnt[0], slots = 64u * F;
     const uint32_t nw = gridDim.x * TOP_WARPS;
-    for (uint32_t it = blockIdx.x * TOP_WARPS + (threadIdx.x >> 5); it < count; it += nw) {
-        const int2 item = __ldg(cv.top + it);
+    for (uint32_t it = blockIdx.x * TOP_WARPS + (threadIdx.x >> 5); it < slots; it += nw) {
+        const uint32_t ch = it % F, sl = it / F;
+        if ((int)sl >= __ldg(cv.rcnt + 3 * ch + 2)) continue;
+        const int2 item = __ldg(cv.top + 64 * ch + sl);
         const int g = item.x, d = item.y, c = g / BUILD_LEAVES;
         if (g < 0 || g > n - 2 || c >= cnt[0]) {
             if (lane == 0) atomicOr(err, ERR_TIMEOUT);
@@ -908,11 +908,11 @@ k_build_top(ChunkView cv, Node* nodes, int2* range, BvhRoot* root, int* err) {
         int2 q;
         int jl = -1, dlft = -1, cl = -1;
         float4 lo = ident_lo(), hi = ident_hi();
-        int k = first_record(cv.srec + 32 * c, __ldg(cv.rcnt + 2 * c), g, d, false, lane, q);
+        int k = first_record(cv.srec + 32 * c, __ldg(cv.rcnt + 3 * c), g, d, false, lane, q);
         int cc = c;
         if (k < 0) {
             cc = nearest_chunk(cv, cnt, c, d, false, lane, err);
-            if (cc >= 0) k = first_record(cv.srec + 32 * cc, __ldg(cv.rcnt + 2 * cc), -1, d, false, lane, q);
+            if (cc >= 0) k = first_record(cv.srec + 32 * cc, __ldg(cv.rcnt + 3 * cc), -1, d, false, lane, q);
         }
         if (k >= 0) {
             jl = q.x;
@@ -922,11 +922,11 @@ k_build_top(ChunkView cv, Node* nodes, int2* range, BvhRoot* root, int* err) {
         }
         // right end: boundary jr (leaves up to jr), n - 1 = none
         int jr = n - 1, drgt = -1, cr = cnt[0] - 1;
-        k = first_record(cv.prec + 32 * c, __ldg(cv.rcnt + 2 * c + 1), g, d, true, lane, q);
+        k = first_record(cv.prec + 32 * c, __ldg(cv.rcnt + 3 * c + 1), g, d, true, lane, q);
         cc = c;
         if (k < 0) {
             cc = nearest_chunk(cv, cnt, c, d, true, lane, err);
-            if (cc >= 0) k = first_record(cv.prec + 32 * cc, __ldg(cv.rcnt + 2 * cc + 1), -1, d, true, lane, q);
+            if (cc >= 0) k = first_record(cv.prec + 32 * cc, __ldg(cv.rcnt + 3 * cc + 1), -1, d, true, lane, q);
         }
         if (k >= 0) {
             jr = q.x;
@@ -989,12 +989,12 @@ void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
     a.want(&sbox, 64 * (size_t)chunks);
     a.want(&prec, 32 * (size_t)chunks);
     a.want(&pbox, 64 * (size_t)chunks);
-    a.want(&rcnt, 2 * (size_t)chunks);
+    a.want(&rcnt, 3 * (size_t)chunks);
     a.want(&top, 64 * (size_t)chunks);
     a.want(&root, 1);
     // histograms | sort status (PASSES x tiles x RADIX) | sort counters | unique status | unique counter
-    // | rebuild mode word | top list count | finished chunk CTAs
-    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 4;
+    // | rebuild mode word | finished chunk CTAs
+    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 3;
     a.want(&scratch, scratch_words);
 }
 
@@ -1008,7 +1008,7 @@ cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_e
     uint32_t* ustat = scount + PASSES;
     uint32_t* ucount = ustat + b.tiles_sort;
     uint32_t* mode = ucount + 1;
-    ChunkView cv{b.cmin, b.cbox, b.srec, b.sbox, b.prec, b.pbox, b.rcnt, b.top, mode + 1, mode + 2,
+    ChunkView cv{b.cmin, b.cbox, b.srec, b.sbox, b.prec, b.pbox, b.rcnt, b.top, mode + 1,
                  {b.lev_off[0], b.lev_off[1], b.lev_off[2], b.lev_off[3]}};
     k_body_prep<<<cdiv(b.nv, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.xyz_in, b.has_normals ? b.nrm_in : nullptr,
                                                                      b.nv, thickness, b.verts, b.root, b.nt);
