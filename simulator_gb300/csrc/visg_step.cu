@@ -623,7 +623,9 @@ cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int ch
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_collide, COLLIDE_BLOCK, 0);
-            g_collide_grid = sms * (occ > 0 ? occ : 1);
+            // two CTAs per SM walk the queue (grid-stride): threads for the usual queue
+            // without idle CTAs competing for slots with the other group's step
+            g_collide_grid = sms * (occ >= 2 ? 2 : 1);
         }
         k_collide<<<g_collide_grid, COLLIDE_BLOCK, 0, s>>>(a);
     }
