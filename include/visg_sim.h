@@ -177,7 +177,7 @@ int visg_render_shaded(VisgSim* sim, float* pos4, float* vertex_normals, float* 
  * copies synchronously every frame): enqueues, behind the steps issued so far, the
  * copy of all n_vertices*3 positions into host memory `out` (page-locked memory
  * lets the copy run asynchronously) and returns at once, so the steps issued next
- * run while the copy proceeds.  At most two reads may be in flight; `out` must
+ * run while the copy proceeds.  At most three reads may be in flight; `out` must
  * stay valid until visg_wait_positions has returned for it.  visg_wait_positions
  * waits for the oldest read in flight and reports device-side errors raised up to
  * the step it read. */

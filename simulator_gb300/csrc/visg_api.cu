@@ -181,20 +181,21 @@ struct Engine {
 
     // asynchronous position read-back: two device staging slots copied to host memory
     // on their own stream while later steps run
+    static constexpr int kReadSlots = 3;  // reads in flight at most
     struct Readback {
         cudaStream_t copy = nullptr;
-        float* d_pos[2] = {nullptr, nullptr};
-        cudaEvent_t unpacked[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+        float* d_pos[kReadSlots] = {};
+        cudaEvent_t unpacked[kReadSlots] = {}, copied[kReadSlots] = {};
         uint32_t* h_err = nullptr;  // pinned: the error word as of each slot's read
-        bool used[2] = {false, false};
+        bool used[kReadSlots] = {};
         int next = 0;     // slot of the next read
-        int pending = 0;  // reads issued and not yet waited for (0..2)
+        int pending = 0;  // reads issued and not yet waited for (0..kReadSlots)
     } rb;
 
     ~Engine() {
         if (stream) cudaStreamSynchronize(stream);
         cudaDeviceSynchronize();
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < kReadSlots; ++k) {
             if (rb.d_pos[k]) cudaFree(rb.d_pos[k]);
             if (rb.unpacked[k]) cudaEventDestroy(rb.unpacked[k]);
             if (rb.copied[k]) cudaEventDestroy(rb.copied[k]);
@@ -781,11 +782,11 @@ struct Engine {
     int read_positions_async(float* out) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
-        if (rb.pending == 2) return fail(VISG_ERR_STATE, "two reads are in flight: wait for one first");
+        if (rb.pending == kReadSlots) return fail(VISG_ERR_STATE, "three reads are in flight: wait for one first");
         if (!rb.copy) {
             CU(cudaStreamCreateWithFlags(&rb.copy, cudaStreamNonBlocking));
-            CU(cudaHostAlloc((void**)&rb.h_err, 16, cudaHostAllocDefault));
-            for (int k = 0; k < 2; ++k) {
+            CU(cudaHostAlloc((void**)&rb.h_err, 4 * kReadSlots, cudaHostAllocDefault));
+            for (int k = 0; k < kReadSlots; ++k) {
                 CU(cudaMalloc((void**)&rb.d_pos[k], (size_t)N * 12 + 16));
                 CU(cudaEventCreateWithFlags(&rb.unpacked[k], cudaEventDisableTiming));
                 CU(cudaEventCreateWithFlags(&rb.copied[k], cudaEventDisableTiming));
@@ -800,7 +801,7 @@ struct Engine {
         CU(cudaMemcpyAsync(out, rb.d_pos[k], (size_t)N * 12, cudaMemcpyDeviceToHost, rb.copy));
         CU(cudaEventRecord(rb.copied[k], rb.copy));
         rb.used[k] = true;
-        rb.next ^= 1;
+        rb.next = (rb.next + 1) % kReadSlots;
         ++rb.pending;
         return VISG_OK;
     }
@@ -808,7 +809,7 @@ struct Engine {
     // wait for the oldest read in flight; reports device-side errors like a sync
     int wait_positions() {
         if (rb.pending == 0) return fail(VISG_ERR_STATE, "no read in flight");
-        const int k = rb.pending == 2 ? rb.next : rb.next ^ 1;
+        const int k = (rb.next - rb.pending + kReadSlots) % kReadSlots;  // the oldest
         --rb.pending;
         CU(cudaEventSynchronize(rb.copied[k]));
         if (rb.h_err[k] != 0u) return sync();  // a device-side error: report it (and clear it)

@@ -493,17 +493,19 @@ def test_pipelined_position_reads_equal_synchronous_reads():
     for k in range(8):
         a.simulate(1)
         a.read_positions_async(got[k])
-        if k > 0:
-            a.wait_positions()
+        if k > 1:
+            a.wait_positions()  # the read of step k - 2
         s.simulate(1)
         want.append(s.positions())
     extra = np.empty((a.n, 3), np.float32)
     a.simulate(1)
-    a.read_positions_async(extra)  # the second read in flight
+    a.read_positions_async(extra)  # the third read in flight
     with pytest.raises(RuntimeError):
-        a.read_positions_async(np.empty((a.n, 3), np.float32))  # a third is refused
-    a.wait_positions()
-    a.wait_positions()
+        a.read_positions_async(np.empty((a.n, 3), np.float32))  # a fourth is refused
+    for _ in range(3):
+        a.wait_positions()
+    with pytest.raises(RuntimeError):
+        a.wait_positions()  # none left
     s.simulate(1)
     assert np.array_equal(extra, s.positions())
     for k in range(8):
