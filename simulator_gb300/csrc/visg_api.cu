@@ -718,7 +718,7 @@ struct Engine {
     }
 
     int set_vertex(int g, uint32_t idx, const float* xyz) {
-        int64_t v;
+        int64_t v = 0;
         if (int r = check_vertex(g, idx, &v)) return r;
         if (!xyz) return fail(VISG_ERR_INVALID_ARG, "xyz is NULL");
         const uint32_t gi = (uint32_t)v;  // x and x_old (simulation.cu:255-256)
