@@ -324,16 +324,16 @@ int visg_obj_load(const char* path, VisgObj** out, int32_t* n_vertices, int32_t*
 
 int visg_obj_get(const VisgObj* o, float* xyz, float* normals, uint32_t* faces) {
     if (!o) return obj_fail(VISG_ERR_INVALID_ARG, "obj is NULL");
-    if (xyz) std::memcpy(xyz, o->xyz.data(), o->xyz.size() * 4);
-    if (normals) std::memcpy(normals, o->normals.data(), o->normals.size() * 4);
-    if (faces) std::memcpy(faces, o->faces.data(), o->faces.size() * 4);
+    if (xyz && !o->xyz.empty()) std::memcpy(xyz, o->xyz.data(), o->xyz.size() * 4);
+    if (normals && !o->normals.empty()) std::memcpy(normals, o->normals.data(), o->normals.size() * 4);
+    if (faces && !o->faces.empty()) std::memcpy(faces, o->faces.data(), o->faces.size() * 4);
     return VISG_OK;
 }
 
 int visg_obj_groups(const VisgObj* o, int32_t* sizes, int32_t* n_groups) {
     if (!o) return obj_fail(VISG_ERR_INVALID_ARG, "obj is NULL");
     if (n_groups) *n_groups = (int32_t)o->groups.size();
-    if (sizes) std::memcpy(sizes, o->groups.data(), o->groups.size() * 4);
+    if (sizes && !o->groups.empty()) std::memcpy(sizes, o->groups.data(), o->groups.size() * 4);
     return VISG_OK;
 }
 

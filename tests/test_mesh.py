@@ -123,3 +123,22 @@ def test_obj_garment_over_obj_body_vs_oracle(tmp_path):
     assert g.count_contacts() > 0
     pos4, vn, fn = g.render()
     assert np.array_equal(pos4[:, :3], x) and np.isfinite(vn).all() and len(fn) == len(cf)
+
+
+def test_obj_reader_empty_parts(tmp_path):
+    """Files without groups, faces or vertices read as empty parts (the copies of
+    empty arrays touch nothing), or are rejected with an error."""
+    p = tmp_path / "nogroups.obj"
+    p.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    assert vs.obj_groups(str(p)).tolist() == []
+    p = tmp_path / "nofaces.obj"
+    p.write_text("v 0 0 0\nv 1 0 0\n")
+    xyz, nrm, faces = vs.load_obj(str(p))
+    assert xyz.shape == (2, 3) and faces.shape == (0, 3)
+    p = tmp_path / "empty.obj"
+    p.write_text("# nothing here\n")
+    try:
+        xyz, nrm, faces = vs.load_obj(str(p))
+        assert len(xyz) == 0 and len(faces) == 0
+    except vs.VisgError:
+        pass
