@@ -17,6 +17,8 @@
 
 #include "visg_internal.cuh"
 
+#include <nvtx3/nvToolsExt.h>  // header-only: the ranges cost nothing unless a profiler attaches
+
 using namespace visg;
 
 namespace {
@@ -1213,6 +1215,14 @@ struct VisgBatch {
 #include "visg_adjoint_host.inl"
 
 // =====================================================================================
+// a named range around each public call, for profilers (NVTX)
+struct ApiRange {
+    explicit ApiRange(const char* name) { nvtxRangePushA(name); }
+    ~ApiRange() { nvtxRangePop(); }
+    ApiRange(const ApiRange&) = delete;
+    ApiRange& operator=(const ApiRange&) = delete;
+};
+
 extern "C" {
 
 void visg_default_params(VisgParams* p) {
@@ -1257,6 +1267,7 @@ int visg_create(const VisgParams* params, const float* cloth_xyz, int32_t n_vert
                 const VisgSpring* const* csr, const float* const* list_k, const float* body_xyz,
                 const float* body_normals, int32_t n_body_vertices, const uint32_t* tris, int32_t n_tris,
                 VisgSim** out) {
+    ApiRange range_("visg_create");
     if (!out) return fail(VISG_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
     if (int r = validate_params(params)) return r;
@@ -1289,16 +1300,19 @@ int visg_set_stream(VisgSim* sim, void* stream) {
 }
 
 int visg_step(VisgSim* sim, int32_t nsteps) {
+    ApiRange range_("visg_step");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.step(nsteps);
 }
 
 int visg_update_body(VisgSim* sim, const float* xyz, const float* nrm) {
+    ApiRange range_("visg_update_body");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.update_body(0, xyz, nrm, cudaMemcpyHostToDevice);
 }
 
 int visg_update_body_device(VisgSim* sim, const float* xyz, const float* nrm) {
+    ApiRange range_("visg_update_body_device");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.update_body(0, xyz, nrm, cudaMemcpyDeviceToDevice);
 }
@@ -1319,11 +1333,13 @@ int visg_set_pinned(VisgSim* sim, const uint32_t* idx, int32_t n) {
 }
 
 int visg_get_positions(VisgSim* sim, float* out, int32_t on_device) {
+    ApiRange range_("visg_get_positions");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.get_positions(0, out, on_device);
 }
 
 int visg_read_positions_async(VisgSim* sim, float* out) {
+    ApiRange range_("visg_read_positions_async");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.read_positions_async(out);
 }
@@ -1340,12 +1356,14 @@ int visg_set_faces(VisgSim* sim, const uint32_t* faces, int32_t n_faces) {
 
 int visg_render(VisgSim* sim, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
                 int32_t normals_of_previous) {
+    ApiRange range_("visg_render");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.render(pos4, vertex_normals, face_normals, nullptr, nullptr, on_device, normals_of_previous);
 }
 
 int visg_render_shaded(VisgSim* sim, float* pos4, float* vertex_normals, float* colors, const float object_rgb[3],
                        int32_t on_device, int32_t normals_of_previous) {
+    ApiRange range_("visg_render_shaded");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.render(pos4, vertex_normals, nullptr, colors, object_rgb, on_device, normals_of_previous);
 }
@@ -1409,11 +1427,13 @@ int visg_query_points(VisgSim* sim, const float* pts, int32_t n, int32_t* leaf, 
 }
 
 int visg_forward(VisgSim* sim, int32_t nsteps, int32_t ckpt) {
+    ApiRange range_("visg_forward");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.forward(nsteps, ckpt);
 }
 
 int visg_backward(VisgSim* sim, const float* dL_dx, const float* dL_dxo, float* dL_dk, float* dL_dscalar) {
+    ApiRange range_("visg_backward");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.backward(dL_dx, dL_dxo, dL_dk, dL_dscalar);
 }
@@ -1441,6 +1461,7 @@ int visg_batch_add(VisgBatch* b, const float* cloth_xyz, int32_t n_vertices, con
 }
 
 int visg_batch_finalize(VisgBatch* b) {
+    ApiRange range_("visg_batch_finalize");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.finalize();
 }
@@ -1452,11 +1473,13 @@ int visg_batch_set_stream(VisgBatch* b, void* stream) {
 }
 
 int visg_batch_step(VisgBatch* b, int32_t nsteps) {
+    ApiRange range_("visg_batch_step");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.step(nsteps);
 }
 
 int visg_batch_get_positions(VisgBatch* b, int32_t garment, float* out, int32_t on_device) {
+    ApiRange range_("visg_batch_get_positions");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.get_positions(garment, out, on_device);
 }
@@ -1472,6 +1495,7 @@ int visg_batch_set_state(VisgBatch* b, int32_t garment, const float* x, const fl
 }
 
 int visg_batch_read_positions_async(VisgBatch* b, float* out) {
+    ApiRange range_("visg_batch_read_positions_async");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.read_positions_async(out);
 }
@@ -1488,12 +1512,14 @@ int visg_batch_set_faces(VisgBatch* b, int32_t garment, const uint32_t* faces, i
 
 int visg_batch_render(VisgBatch* b, float* pos4, float* vertex_normals, float* face_normals, int32_t on_device,
                       int32_t normals_of_previous) {
+    ApiRange range_("visg_batch_render");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.render(pos4, vertex_normals, face_normals, nullptr, nullptr, on_device, normals_of_previous);
 }
 
 int visg_batch_render_shaded(VisgBatch* b, float* pos4, float* vertex_normals, float* colors,
                              const float object_rgb[3], int32_t on_device, int32_t normals_of_previous) {
+    ApiRange range_("visg_batch_render_shaded");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.render(pos4, vertex_normals, nullptr, colors, object_rgb, on_device, normals_of_previous);
 }
@@ -1509,11 +1535,13 @@ int visg_batch_set_vertices(VisgBatch* b, const uint32_t* idx, const float* xyz,
 }
 
 int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* xyz, const float* nrm) {
+    ApiRange range_("visg_batch_update_body");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.update_body(garment, xyz, nrm, cudaMemcpyHostToDevice);
 }
 
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas) {
+    ApiRange range_("visg_batch_autotune");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.autotune(block, ctas);
 }
