@@ -379,6 +379,16 @@ int visg_mesh_rotate(float* xyz, int32_t n, float angle_degrees, int32_t axis);
 #define VISG_NOALLOC_MAX_VERTICES 32768
 #define VISG_NOALLOC_MAX_TRIS 32768
 #define VISG_NOALLOC_SCRATCH_BYTES (9u * 1024u * 1024u)
+/* Self-test of the device-side failure detection: runs, on the current device, one
+ * kernel that waits on an mbarrier phase nothing completes (the wait of the step's
+ * shared-memory staging ring) and one that looks back at a radix-sort status word
+ * nothing publishes (the wait of the LBVH's radix passes and de-duplication).  Each
+ * wait is bounded and must give up, record the timeout and return; *gave_up gets
+ * bit 0 for the first, bit 1 for the second (3 = both behaved).  Returns VISG_OK when
+ * the device is still usable afterwards.  Takes about a second (the staging wait's
+ * limit).  No counterpart in the reference. */
+int visg_selftest_bounded_waits(int32_t* gave_up);
+
 int visg_lbvh_build_noalloc(const float* d_xyz, const float* d_normals, int32_t n_vertices,
                             const uint32_t* d_tris, int32_t n_tris, float thickness, float box_depth,
                             uint32_t* d_sorted_codes, int32_t* d_sorted_tris,

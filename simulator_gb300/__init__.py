@@ -51,6 +51,7 @@ def lib():
     sig = {
         "visg_default_params": (None, [C.POINTER(VisgParams)]),
         "visg_version": (C.c_char_p, []),
+        "visg_selftest_bounded_waits": (C.c_int, [_i32p]),
         "visg_last_error": (C.c_char_p, []),
         "visg_create": (C.c_int, [C.POINTER(VisgParams), _fp, C.c_int32, C.POINTER(_u32p), C.POINTER(_vp),
                                   C.POINTER(_fp), _fp, _fp, C.c_int32, _u32p, C.c_int32, C.POINTER(_vp)]),
@@ -457,6 +458,15 @@ class BatchSimulator:
             self.close()
         except Exception:
             pass
+
+
+def selftest_bounded_waits() -> int:
+    """Run the device-side failure-detection self-test (visg_selftest_bounded_waits):
+    a staging-ring wait and a radix look-back wait that nothing completes must both
+    give up and report it.  Returns the bits of the waits that gave up (3 = both)."""
+    bits = C.c_int32()
+    _check(lib().visg_selftest_bounded_waits(C.byref(bits)))
+    return bits.value
 
 
 def springs_from_mesh(xyz, tris):

@@ -1540,6 +1540,30 @@ int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* xyz, cons
     return b->eng.update_body(garment, xyz, nrm, cudaMemcpyHostToDevice);
 }
 
+int visg_selftest_bounded_waits(int32_t* gave_up) {
+    ApiRange range_("visg_selftest_bounded_waits");
+    if (!gave_up) return fail(VISG_ERR_INVALID_ARG, "gave_up is NULL");
+    *gave_up = 0;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return fail(VISG_ERR_NO_DEVICE, "no CUDA device");
+    int* d = nullptr;  // [0] mbarrier wait's error word, [1] look-back's, [2] a status word nothing publishes
+    cudaError_t e = cudaMalloc((void**)&d, 16);
+    if (e != cudaSuccess) return cuda_fail(e, "self-test buffer");
+    int h[2] = {0, 0};
+    e = cudaMemset(d, 0, 16);
+    if (e == cudaSuccess) e = launch_selftest_mbar_wait(d, nullptr);
+    if (e == cudaSuccess) e = launch_selftest_look_back(reinterpret_cast<const uint32_t*>(d + 2), d + 1, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    // the device must still work after both waits gave up
+    if (e == cudaSuccess) e = cudaMemset(d, 0, 16);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "self-test of the bounded waits");
+    *gave_up = ((h[0] & ERR_TIMEOUT) ? 1 : 0) | ((h[1] & ERR_TIMEOUT) ? 2 : 0);
+    return VISG_OK;
+}
+
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas) {
     ApiRange range_("visg_batch_autotune");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");

@@ -186,6 +186,10 @@ int step_smem_bytes(int variant, int win_cap);
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
 int step_max_ctas_per_sm(int variant, int block, int win_cap);
 
+// self-tests of the bounded waits: each must give up and set ERR_TIMEOUT in *err
+cudaError_t launch_selftest_mbar_wait(int* err, cudaStream_t s);
+cudaError_t launch_selftest_look_back(const uint32_t* zero_status, int* err, cudaStream_t s);
+
 // first-hit queries of external points against one body
 cudaError_t launch_query(BvhView v, const float* pts, int n, int* leaf, int* inside, float* dist,
                          float* normal, int* err, cudaStream_t s);

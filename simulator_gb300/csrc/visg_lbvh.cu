@@ -998,6 +998,20 @@ void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
     a.want(&scratch, scratch_words);
 }
 
+namespace {
+// Self-test of the look-back's bounded wait: one thread looks back from tile 1 at a
+// status word (tile 0's) that nothing publishes; the walk gives up after SPIN_LIMIT
+// sleeps, records ERR_TIMEOUT and returns.
+__global__ void k_selftest_look_back(const uint32_t* status, int* err) {
+    if (threadIdx.x == 0) (void)look_back(status, 1, 1, err);
+}
+}  // namespace
+
+cudaError_t launch_selftest_look_back(const uint32_t* zero_status, int* err, cudaStream_t s) {
+    k_selftest_look_back<<<1, 32, 0, s>>>(zero_status, err);
+    return cudaGetLastError();
+}
+
 cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s) {
     if (b.nt == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(b.scratch, 0, b.scratch_words * sizeof(uint32_t), s);

@@ -783,6 +783,26 @@ inline unsigned grid_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b);
 
 }  // namespace
 
+namespace {
+// Self-test of the staging ring's bounded wait: thread 0 waits on the phase of an
+// mbarrier that nothing arrives on; the wait gives up after kWaitNs and the kernel
+// records ERR_TIMEOUT and returns (no copy is in flight).
+__global__ void k_selftest_mbar_wait(int* err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_addr(&bar), 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait(smem_addr(&bar), 0u)) atomicOr(err, ERR_TIMEOUT);
+}
+}  // namespace
+
+cudaError_t launch_selftest_mbar_wait(int* err, cudaStream_t s) {
+    k_selftest_mbar_wait<<<1, 32, 0, s>>>(err);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s) {
     if (a.n_tiles == 0) return cudaSuccess;
     if (grid <= 0 || grid > a.n_tiles) grid = a.n_tiles;

@@ -710,3 +710,13 @@ def test_trajectory_matches_reference_kernels():
     print(f"200 steps vs reference kernels: max |dx| = {np.abs(x - rx).max():.3e}")
     assert np.abs(x - rx).max() <= TRAJ_TOL
     assert (np.abs(rn).sum(1) > 0).sum() > 10
+
+
+def test_bounded_waits_give_up_and_leave_the_device_usable():
+    """Failure detection without a fault: a staging-ring wait and a radix look-back
+    wait that nothing completes give up (bounded), report ERR_TIMEOUT, and the
+    simulator works normally afterwards."""
+    assert vs.selftest_bounded_waits() == 3
+    cloth, cl, body, p = ref_scene(side=16, subdiv=2)
+    g, o = run_pair(cloth, cl, body, p, 20)
+    assert_state_equal(g, o)
