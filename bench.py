@@ -22,7 +22,9 @@ Reported (one JSON line, rank 0):
               with the host link's own device-to-host rate for the same bytes
               (its ceiling: every step moves all positions over the link)
   plain_loop  the same garments as 256 plain simulators stepped one after another
-  roofline    the fused step kernel: algorithmic bytes per launch / launch time
+  roofline    the fused step kernel: algorithmic bytes per launch / its launch time
+              (CUDA events around each launch, 10 steps as one chain after the timed
+              region; the same over the whole step is kept beside it)
   cpu_baseline the CPU restatement (OpenMP) on the same garments, bounded sample
   moving_body_configs  the plain configurations whose body moves (LBVH rebuilt
               every step), over their stated durations
@@ -399,6 +401,9 @@ def main():
     ms = max_over_ranks(e0.elapsed_time(e1))
     value = nv_all * args.steps / (ms / 1e3)
     contacts = b.count_contacts()
+    # the roofline kernel's own launch time: 10 more steps as one chain (each launch
+    # over the whole batch), CUDA events right around each launch on its stream
+    k_step_ms, k_collide_ms = b.time_kernels(10)
 
     # ---- end to end through the C ABI with host buffers --------------------------------
     # three page-locked result buffers: step k's positions are copied to host memory
@@ -482,8 +487,9 @@ def main():
     # list (L = 1) and 8-byte entries (s = 8): x, x_old, normal read and written as
     # 12-byte vectors, the row offset, and one entry per directed spring
     alg_bytes = 72 * nv + 4 * (nv + 1) + 8 * ne
-    t_launch = ms / 1e3 / args.steps
+    t_launch = k_step_ms / 1e3
     achieved = alg_bytes / t_launch / 1e9
+    achieved_step = alg_bytes / (ms / 1e3 / args.steps) / 1e9  # over the whole step (both kernels)
     peak, peak_kind = peak_hbm()
     traffic = committed_traffic()
 
@@ -512,7 +518,10 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_step (fused integrate + springs + collision)",
-                         "algorithmic_bytes_per_launch": alg_bytes},
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "launch_ms": k_step_ms, "achieved_over_whole_step": achieved_step},
+            "kernel_ms": {"k_step": k_step_ms, "k_collide": k_collide_ms,
+                          "how": "one chain, CUDA events around each launch, mean of 10"},
             "cpu_baseline": cpu,
             "moving_body_configs": moving,
             "adjoint_config": adjoint,

@@ -292,6 +292,12 @@ int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas_per_sm);
  * parameters or visg_batch_autotune), and the kernels one step launches. */
 int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm, int32_t* split_collision,
                            int32_t* stage_neighbours, int32_t* kernels_per_step);
+/* Steps the batch nsteps times as one chain of kernels (each launch covers every
+ * garment), with CUDA events right around each launch of the step kernel and after
+ * each collision pass on the step stream, and returns the average device time in
+ * milliseconds per launch of each (ms_collide_kernel may be NULL; 0 without split
+ * collision).  The steps are real steps of the simulation.  For measurement. */
+int visg_batch_time_kernels(VisgBatch* b, int32_t nsteps, float* ms_step_kernel, float* ms_collide_kernel);
 int visg_batch_info(VisgBatch* b, int32_t* n_garments, int64_t* n_vertices,
                     int64_t* n_entries, int64_t* n_tris);
 int visg_batch_count_contacts(VisgBatch* b, int64_t* n);

@@ -52,6 +52,7 @@ def lib():
         "visg_default_params": (None, [C.POINTER(VisgParams)]),
         "visg_version": (C.c_char_p, []),
         "visg_selftest_bounded_waits": (C.c_int, [_i32p]),
+        "visg_batch_time_kernels": (C.c_int, [_vp, C.c_int32, _fp, _fp]),
         "visg_last_error": (C.c_char_p, []),
         "visg_create": (C.c_int, [C.POINTER(VisgParams), _fp, C.c_int32, C.POINTER(_u32p), C.POINTER(_vp),
                                   C.POINTER(_fp), _fp, _fp, C.c_int32, _u32p, C.c_int32, C.POINTER(_vp)]),
@@ -410,6 +411,13 @@ class BatchSimulator:
 
     def update_body(self, garment: int, xyz, normals=None):
         _check(lib().visg_batch_update_body(self.h, garment, _p(_f32(xyz)), _p(_f32(normals))))
+
+    def time_kernels(self, nsteps: int = 10):
+        """Step nsteps times as one chain with CUDA events around each kernel launch:
+        (ms per step-kernel launch, ms per collision pass), device time averages."""
+        a, c = C.c_float(), C.c_float()
+        _check(lib().visg_batch_time_kernels(self.h, nsteps, C.byref(a), C.byref(c)))
+        return a.value, c.value
 
     def autotune(self):
         b, c = C.c_int32(), C.c_int32()

@@ -651,6 +651,40 @@ struct Engine {
         return VISG_OK;
     }
 
+    // n steps as one chain (each launch covers the whole batch), with CUDA events right
+    // around each step-kernel launch and after each collision pass on the step stream:
+    // the average device time per launch of each kernel
+    int time_kernels(int n, float* ms_step, float* ms_collide) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (n <= 0 || !ms_step) return fail(VISG_ERR_INVALID_ARG, "nsteps <= 0 or ms_step is NULL");
+        cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+        for (auto& x : ev) CU(cudaEventCreate(&x));
+        const int saved = p.overlap_groups;
+        p.overlap_groups = 1;
+        double ts = 0.0, tc = 0.0;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < n && e == cudaSuccess; ++k) {
+            set_step_timing(ev[0], ev[1]);
+            e = launch_step(args(cur, block, 0), variant(block), block, grid, stream);
+            set_step_timing(nullptr, nullptr);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[2], stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
+            float a = 0.0f, b = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&a, ev[0], ev[1]);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&b, ev[1], ev[2]);
+            ts += a;
+            tc += b;
+            cur ^= 1;
+        }
+        p.overlap_groups = saved;
+        prev_ok = true;
+        for (auto& x : ev) cudaEventDestroy(x);
+        if (e != cudaSuccess) return cuda_fail(e, "kernel timing");
+        *ms_step = (float)(ts / n);
+        if (ms_collide) *ms_collide = (variant(block) & SV_SPLIT) ? (float)(tc / n) : 0.0f;
+        return sync();
+    }
+
     // wait, then report device-side errors (and the divergence check)
     int sync() {
         CU(cudaMemcpyAsync(h_status, d_err, 4, cudaMemcpyDeviceToHost, stream));
@@ -1538,6 +1572,12 @@ int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* xyz, cons
     ApiRange range_("visg_batch_update_body");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return b->eng.update_body(garment, xyz, nrm, cudaMemcpyHostToDevice);
+}
+
+int visg_batch_time_kernels(VisgBatch* b, int32_t nsteps, float* ms_step_kernel, float* ms_collide_kernel) {
+    ApiRange range_("visg_batch_time_kernels");
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.time_kernels(nsteps, ms_step_kernel, ms_collide_kernel);
 }
 
 int visg_selftest_bounded_waits(int32_t* gave_up) {

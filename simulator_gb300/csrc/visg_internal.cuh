@@ -184,6 +184,8 @@ enum StepVariant : int {
 // dynamic shared memory of a launch: two stage buffers of win_cap entries + barriers
 int step_smem_bytes(int variant, int win_cap);
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s);
+// record `before` / `after` around every step-kernel launch this thread issues (null: stop)
+void set_step_timing(cudaEvent_t before, cudaEvent_t after);
 int step_max_ctas_per_sm(int variant, int block, int win_cap);
 
 // self-tests of the bounded waits: each must give up and set ERR_TIMEOUT in *err

@@ -606,6 +606,10 @@ cudaError_t allow_smem(const void* fn, int bytes) {
     return e;
 }
 
+// events recorded right before and after each step-kernel launch of this thread
+// (kernel timing; null = none)
+thread_local cudaEvent_t t_before_step = nullptr, t_after_step = nullptr;
+
 template <int BLOCK, bool KD0, bool STAGED>
 cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int check, int perk, int grid, int smem,
                       cudaStream_t s) {
@@ -616,7 +620,9 @@ cudaError_t launch_kd(const StepArgs& a, bool coll, bool split, int refv, int ch
         e = cudaMemsetAsync(a.cand_count, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
     }
+    if (t_before_step) cudaEventRecord(t_before_step, s);
     fn<<<grid, BLOCK, smem, s>>>(a, refv, check, perk);
+    if (t_after_step) cudaEventRecord(t_after_step, s);
     if (coll && split) {
         if (g_collide_grid == 0) {
             int dev = 0, sms = 0, occ = 0;
@@ -801,6 +807,11 @@ __global__ void k_selftest_mbar_wait(int* err) {
 cudaError_t launch_selftest_mbar_wait(int* err, cudaStream_t s) {
     k_selftest_mbar_wait<<<1, 32, 0, s>>>(err);
     return cudaGetLastError();
+}
+
+void set_step_timing(cudaEvent_t before, cudaEvent_t after) {
+    t_before_step = before;
+    t_after_step = after;
 }
 
 cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cudaStream_t s) {

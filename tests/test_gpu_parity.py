@@ -720,3 +720,25 @@ def test_bounded_waits_give_up_and_leave_the_device_usable():
     cloth, cl, body, p = ref_scene(side=16, subdiv=2)
     g, o = run_pair(cloth, cl, body, p, 20)
     assert_state_equal(g, o)
+
+
+def test_batch_kernel_timing_steps_like_step():
+    """visg_batch_time_kernels steps the batch (one chain, events around each kernel):
+    the trajectory equals plain steps, and both kernel times are positive."""
+    items = scenes.garment_batch(4, seed=2, side_range=(16, 40), subdiv_range=(2, 3))
+    out = []
+    for timed in (True, False):
+        b = vs.BatchSimulator(scenes.physics_params(4))
+        for cloth, body in items:
+            b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+        b.finalize()
+        b.step(20)
+        if timed:
+            ks, kc = b.time_kernels(7)
+            assert ks > 0.0 and kc > 0.0
+        else:
+            b.step(7)
+        out.append(b.state())
+        b.close()
+    for u, v in zip(*out):
+        assert np.array_equal(u, v)
