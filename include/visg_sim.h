@@ -236,7 +236,8 @@ int visg_backward(VisgSim* sim, const float* dL_dx, const float* dL_dxold,
                   float* dL_dk, float* dL_dscalar);
 
 /* ======================================================================== */
-/* Batched form: many garments, each with its own body, one launch per step.  */
+/* Batched form: many garments, each with its own body; every launch covers many garments
+ * (two garment groups as overlapping chains of kernels per step by default).  */
 /* ======================================================================== */
 typedef struct VisgBatch VisgBatch;
 

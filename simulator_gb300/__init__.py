@@ -327,7 +327,8 @@ class Simulator:
 
 
 class BatchSimulator:
-    """Many garments, each with its own body, stepped by one launch per step."""
+    """Many garments, each with its own body; every kernel launch covers many garments
+    (by default two garment groups, each its own overlapping chain of kernels)."""
 
     def __init__(self, params: VisgParams):
         L = lib()
