@@ -371,13 +371,16 @@ int visg_mesh_rotate(float* xyz, int32_t n, float angle_degrees, int32_t axis);
  * allocation of any kind.
  *
  *   d_xyz / d_normals   n_vertices*3 floats (normals may be NULL: no thickness push)
- *   d_tris              n_tris*3 vertex indices, each < n_vertices (not checked)
+ *   d_tris              n_tris*3 vertex indices, each < n_vertices; checked on the device:
+ *                       an index out of range is never used to read a vertex, and the
+ *                       call's result is then reported as failed (*d_n_leaves = -1)
  *   outputs (device):   d_sorted_codes[n_tris], d_sorted_tris[n_tris] — the first T'
  *                       entries are the de-duplicated Morton order;
  *                       d_child_a/d_child_b[n_tris-1] — the first T'-1 entries are the
  *                       radix tree's links in the reference's encoding (as
  *                       visg_export_lbvh returns them); d_n_leaves[1] = T', or -1 if a
- *                       bounded device wait gave up.
+ *                       bounded device wait gave up or an index was out of range (the
+ *                       other outputs are then undefined).
  * Limits: n_vertices <= VISG_NOALLOC_MAX_VERTICES, n_tris <= VISG_NOALLOC_MAX_TRIS;
  * larger bodies return VISG_ERR_INVALID_ARG.  Asynchronous on `cuda_stream`.  The
  * first call on a device looks up the static array's device address

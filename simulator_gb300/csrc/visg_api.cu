@@ -700,6 +700,7 @@ struct Engine {
             CU(cudaStreamSynchronize(stream));
             if (err & ERR_TIMEOUT) return fail(VISG_ERR_TIMEOUT, "a bounded device wait gave up (LBVH look-back or step stage copy)");
             if (err & ERR_STACK) return fail(VISG_ERR_UNSUPPORTED, "BVH deeper than the traversal stack");
+            if (err & ERR_INDEX) return fail(VISG_ERR_INVALID_ARG, "an index read on the device was out of range");
             char buf[160];
             std::snprintf(buf, sizeof buf, "diverged: %u non-finite vertices, max step displacement %g (limit %g)", bad,
                           (double)maxd, (double)p.max_displacement);

@@ -54,6 +54,7 @@ constexpr uint32_t FLAG_LEAF_CACHED = 4u; // the query cache's answer is the lea
 constexpr int ERR_STACK = 1;     // traversal stack would overflow (not reachable for <= 30-bit codes)
 constexpr int ERR_DIVERGED = 2;  // divergence check tripped
 constexpr int ERR_TIMEOUT = 4;   // a bounded look-back wait gave up
+constexpr int ERR_INDEX = 8;     // an index read on the device was out of range (not used as one)
 
 // LBVH internal node: children's boxes and links.  Links: >= 0 internal node,
 // < 0 leaf ~link.  Each child writes its own two float4 during the build.

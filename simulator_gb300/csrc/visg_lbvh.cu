@@ -156,15 +156,25 @@ __device__ __forceinline__ void box_add(f3& lo, f3& hi, f3 p) {
 }
 
 __global__ void __launch_bounds__(BUILD_THREADS)
-k_tri_boxes(const float4* __restrict__ verts, const uint32_t* __restrict__ tris, int nt, float depth,
-            float4* __restrict__ tri_box, float4* __restrict__ tri_leaf, BvhRoot* root) {
+k_tri_boxes(const float4* __restrict__ verts, int nv, const uint32_t* __restrict__ tris, int nt, float depth,
+            float4* __restrict__ tri_box, float4* __restrict__ tri_leaf, BvhRoot* root, int* err) {
     __shared__ float s_red[6][BUILD_THREADS / 32];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     f3 lo = mk3(100.0f, 100.0f, 100.0f), hi = mk3(-100.0f, -100.0f, -100.0f);
     if (t < nt) {
-        f3 v0 = xyz(__ldg(&verts[tris[3 * t]]));
-        f3 v1 = xyz(__ldg(&verts[tris[3 * t + 1]]));
-        f3 v2 = xyz(__ldg(&verts[tris[3 * t + 2]]));
+        // vertex indices come from the caller: one out of range is recorded and read
+        // as vertex 0, so no load leaves the vertex array (the build's result is then
+        // reported as failed)
+        uint32_t i0 = tris[3 * t], i1 = tris[3 * t + 1], i2 = tris[3 * t + 2];
+        if (i0 >= (uint32_t)nv || i1 >= (uint32_t)nv || i2 >= (uint32_t)nv) {
+            atomicOr(err, ERR_INDEX);
+            i0 = i0 < (uint32_t)nv ? i0 : 0u;
+            i1 = i1 < (uint32_t)nv ? i1 : 0u;
+            i2 = i2 < (uint32_t)nv ? i2 : 0u;
+        }
+        f3 v0 = xyz(__ldg(&verts[i0]));
+        f3 v1 = xyz(__ldg(&verts[i1]));
+        f3 v2 = xyz(__ldg(&verts[i2]));
         f3 n = normalize(cross(sub(v1, v0), sub(v2, v0)));  // Primitive::d_get_normal
         f3 blo = v0, bhi = v0;                                 // BBox(v0).expand(v1).expand(v2)
         box_add(blo, bhi, v1);
@@ -1026,8 +1036,8 @@ cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_e
                  {b.lev_off[0], b.lev_off[1], b.lev_off[2], b.lev_off[3]}};
     k_body_prep<<<cdiv(b.nv, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.xyz_in, b.has_normals ? b.nrm_in : nullptr,
                                                                      b.nv, thickness, b.verts, b.root, b.nt);
-    k_tri_boxes<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.verts, b.tris, b.nt, box_depth, b.tri_box,
-                                                                     b.tri_leaf, b.root);
+    k_tri_boxes<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.verts, b.nv, b.tris, b.nt, box_depth, b.tri_box,
+                                                                     b.tri_leaf, b.root, d_err);
     k_morton<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.tri_box, b.nt, b.root, b.codes, ghist);
     if (b.coherent)
         k_coherence<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.codes, b.keys[1], b.vals[1], b.nt, b.root,

@@ -58,13 +58,27 @@ int scratch_address(void** out) {
 // Reference layout of the links (BRTreeNode, cudaBRT.h:34-115): the root is
 // internal node 0; an internal node that is child A takes the index of its last
 // leaf, child B of its first.  Pass 1 gives every internal node its index.
+// Both passes run only on a build that reported no error, and check every index
+// they read from the tree before using it: a build whose bounded wait gave up can
+// leave the shared array with another call's nodes, and nothing read from there may
+// send a store outside the caller's arrays.  A bad index sets ERR_INDEX instead.
+__device__ __forceinline__ bool tree_ok(const BvhRoot* root, const int* err, int n_tris, int& n) {
+    n = root->n_leaves;
+    return *err == 0 && n >= 2 && n <= n_tris;
+}
+
 __global__ void k_karras_index(const Node* __restrict__ nodes, const int2* __restrict__ range,
-                               const BvhRoot* __restrict__ root, int* __restrict__ kidx) {
-    const int n = root->n_leaves;
+                               const BvhRoot* __restrict__ root, int* __restrict__ kidx, int n_tris, int* err) {
+    int n;
+    if (!tree_ok(root, err, n_tris, n)) return;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n - 1) return;
     if (g == root->root) kidx[g] = 0;
     const int la = __float_as_int(nodes[g].a_lo.w), lb = __float_as_int(nodes[g].b_lo.w);
+    if (la >= n - 1 || lb >= n - 1) {
+        atomicOr(err, ERR_INDEX);
+        return;
+    }
     if (la >= 0) kidx[la] = range[la].y;
     if (lb >= 0) kidx[lb] = range[lb].x;
 }
@@ -72,17 +86,23 @@ __global__ void k_karras_index(const Node* __restrict__ nodes, const int2* __res
 // Pass 2: child links in the reference encoding (+(i+1) internal, -(i+1) leaf).
 __global__ void k_karras_links(const Node* __restrict__ nodes, const BvhRoot* __restrict__ root,
                                const int* __restrict__ kidx, int32_t* __restrict__ child_a,
-                               int32_t* __restrict__ child_b) {
-    const int n = root->n_leaves;
+                               int32_t* __restrict__ child_b, int n_tris, int* err) {
+    int n;
+    if (!tree_ok(root, err, n_tris, n)) return;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n - 1) return;
     const int k = kidx[g];
     const int la = __float_as_int(nodes[g].a_lo.w), lb = __float_as_int(nodes[g].b_lo.w);
+    if (k < 0 || k >= n - 1 || la >= n - 1 || lb >= n - 1) {
+        atomicOr(err, ERR_INDEX);
+        return;
+    }
     child_a[k] = la < 0 ? -(~la) - 1 : kidx[la] + 1;
     child_b[k] = lb < 0 ? -(~lb) - 1 : kidx[lb] + 1;
 }
 
-// Leaf count to the caller; -1 if a bounded wait of the build gave up.
+// Leaf count to the caller; -1 if a bounded wait of the build gave up or an index
+// was out of range (a triangle's vertex index, or one read from the tree).
 __global__ void k_report(const BvhRoot* __restrict__ root, const int* __restrict__ err, int32_t* n_leaves) {
     *n_leaves = *err ? -1 : root->n_leaves;
 }
@@ -131,8 +151,8 @@ extern "C" int visg_lbvh_build_noalloc(const float* d_xyz, const float* d_normal
     if (e == cudaSuccess) e = lbvh_build(b, thickness, box_depth, d_err, s);
     if (e == cudaSuccess && n_tris > 1) {
         const unsigned grid = (unsigned)((n_tris + 255) / 256);
-        k_karras_index<<<grid, 256, 0, s>>>(b.nodes, b.range, b.root, kidx);
-        k_karras_links<<<grid, 256, 0, s>>>(b.nodes, b.root, kidx, d_child_a, d_child_b);
+        k_karras_index<<<grid, 256, 0, s>>>(b.nodes, b.range, b.root, kidx, n_tris, d_err);
+        k_karras_links<<<grid, 256, 0, s>>>(b.nodes, b.root, kidx, d_child_a, d_child_b, n_tris, d_err);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
