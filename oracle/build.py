@@ -26,7 +26,10 @@ REF_OUT = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(REF_OUT, "refkern.cubin")
 ORACLE_SO = os.path.join(BUILD, "libvisg_oracle.so")
 HARNESS_SO = os.path.join(BUILD, "librefharness.so")
-REFERENCE = os.environ.get("VISG_REFERENCE_DIR", "/root/reference")
+# the reference tree: VISG_REFERENCE_DIR, else a checkout named "reference" beside
+# the repository
+REFERENCE = os.environ.get("VISG_REFERENCE_DIR",
+                           os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 

@@ -42,6 +42,8 @@ def lib():
         L.orc_sim_set_state.argtypes = [C.c_void_p, _fp, _fp, _fp]
         L.orc_sim_n_leaves.argtypes = [C.c_void_p]
         L.orc_sim_n_leaves.restype = C.c_int
+        L.orc_sim_contact_hash.argtypes = [C.c_void_p]
+        L.orc_sim_contact_hash.restype = C.c_uint64
         L.orc_sim_export_lbvh.argtypes = [C.c_void_p, _u32p, _fp, _u32p, _i32p, _i32p, _i32p, _i32p, _i32p,
                                           _fp, _fp, _fp]
         L.orc_sim_query.argtypes = [C.c_void_p, _fp, C.c_int, _i32p, _i32p, _dp, _dp]
@@ -116,6 +118,11 @@ class OracleSim:
 
     def step(self, n: int = 1):
         lib().orc_sim_step(self.h, n)
+
+    def contact_hash(self) -> int:
+        """Running hash of every step's contact set (projected vertices and their
+        normals) since creation: equal hashes = equal contact sets in every step."""
+        return int(lib().orc_sim_contact_hash(self.h))
 
     def update_body(self, xyz, normals=None):
         xyz = np.ascontiguousarray(xyz, np.float32)
@@ -258,6 +265,8 @@ def hlib():
         L.ref_sim_get_state.argtypes = [C.c_void_p, _fp, _fp, _fp]
         L.ref_sim_set_state.argtypes = [C.c_void_p, _fp, _fp, _fp]
         L.ref_sim_n_leaves.argtypes = [C.c_void_p]
+        L.ref_sim_refit_race.argtypes = [C.c_void_p, C.c_int]
+        L.ref_sim_refit_race.restype = C.c_longlong
         L.ref_sim_export_lbvh.argtypes = [C.c_void_p, _u32p, _fp, _u32p, _i32p, _i32p, _i32p, _i32p, _i32p, _fp,
                                           _fp, _fp]
         L.ref_render.argtypes = [_fp, _fp, C.c_int, _u32p, C.c_int, _fp, _fp, _fp]
@@ -324,6 +333,12 @@ class RefSim:
 
     def step(self, n=1):
         self._ok(hlib().ref_sim_step(self.h, n))
+
+    def refit_race(self, repair=None) -> int:
+        """Internal boxes the reference's unfenced refit got wrong, over all builds so
+        far; repair=True makes later builds replace them by the boxes the refit's
+        definition gives (the other kernels then run on the defined tree)."""
+        return int(hlib().ref_sim_refit_race(self.h, -1 if repair is None else int(bool(repair))))
 
     def update_body(self, xyz, normals=None):
         xyz = np.ascontiguousarray(xyz, np.float32)

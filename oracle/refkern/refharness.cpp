@@ -174,6 +174,51 @@ struct RefBvh {
         if (launch(f_refit, (nleaf + 1023) / 1024, 1024, a6)) return -1;
         cudaFree(d_sc);
         cudaFree(d_sb);
+        return check_refit();
+    }
+
+    // calculateBoudingBox (cudaBRT.cu:166-206) reads a sibling's box after atomicInc
+    // without a fence, so now and then an internal box misses part of a child (a
+    // stale read).  Its definition, evaluated here on the host over the reference's
+    // own links and leaf boxes: every internal box is the identity box expanded by
+    // child A's box, then child B's, children first.  Boxes that differ are counted
+    // in `stale`; with `repair` the defined boxes replace the raced ones on the
+    // device, so that every other kernel of the reference runs on the tree its
+    // refit defines.
+    int64_t stale = 0;
+    bool repair = false;
+    int check_refit() {
+        const int ni = Tp - 1;
+        std::vector<RNode> leaf(Tp), in(ni);
+        RT(cudaMemcpy(leaf.data(), d_leaf, sizeof(RNode) * Tp, cudaMemcpyDeviceToHost));
+        RT(cudaMemcpy(in.data(), d_int, sizeof(RNode) * ni, cudaMemcpyDeviceToHost));
+        std::vector<RBBox> def(ni);
+        std::vector<char> done(ni, 0);
+        std::vector<int> stack{0};
+        auto box = [&](int c) -> const RBBox& { return c < 0 ? leaf[-c - 1].bbox : def[c - 1]; };
+        while (!stack.empty()) {
+            const int i = stack.back();
+            const int ca = in[i].childA, cb = in[i].childB;
+            if (ca == 0 || cb == 0 || ca > ni || cb > ni || ca < -Tp || cb < -Tp) return fail("refit check: bad link");
+            bool ready = true;
+            if (ca > 0 && !done[ca - 1]) { stack.push_back(ca - 1); ready = false; }
+            if (cb > 0 && !done[cb - 1]) { stack.push_back(cb - 1); ready = false; }
+            if (!ready) continue;
+            stack.pop_back();
+            RBBox b = identity();
+            expand(b, box(ca));
+            expand(b, box(cb));
+            def[i] = b;
+            done[i] = 1;
+        }
+        int64_t n_stale = 0;
+        for (int i = 0; i < ni; ++i)
+            if (std::memcmp(&def[i], &in[i].bbox, sizeof(RBBox)) != 0) {
+                ++n_stale;
+                in[i].bbox = def[i];
+            }
+        stale += n_stale;
+        if (repair && n_stale) RT(cudaMemcpy(d_int, in.data(), sizeof(RNode) * ni, cudaMemcpyHostToDevice));
         return 0;
     }
 };
@@ -389,6 +434,15 @@ int ref_sim_set_state(void* h, const float* x, const float* xo, const float* n) 
 }
 
 int ref_sim_n_leaves(void* h) { return ((RefSim*)h)->bvh.Tp; }
+
+// Refit race: repair = 1 makes every later build replace the internal boxes its
+// unfenced refit got wrong by the ones its definition gives; the count of wrong
+// boxes found in all builds so far is returned either way.
+long long ref_sim_refit_race(void* h, int repair) {
+    auto* s = (RefSim*)h;
+    if (repair >= 0) s->bvh.repair = repair != 0;
+    return (long long)s->bvh.stale;
+}
 
 // LBVH in the layout of visg_export_lbvh (link fields as BRTreeNode encodes them)
 int ref_sim_export_lbvh(void* h, uint32_t* tri_codes, float* tri_boxes, uint32_t* sorted_codes, int32_t* sorted_tris,

@@ -196,9 +196,51 @@ inline int find_split(const uint32_t* c, int first, int last) {
     return split;
 }
 
+// calculateBoudingBox's result for the subtree under internal node i: every
+// internal box is the identity box expanded by child A's box, then child B's,
+// children before parents.  The top levels' subtrees run as parallel tasks (they
+// share no node); below, one iterative post-order walk per subtree.
+void refit_subtree(Lbvh& b, int i, int level) {
+    auto child_box = [&](int c) -> const Box& { return c < 0 ? b.leaf_box[-c - 1] : b.int_box[c - 1]; };
+    if (level < 10) {
+        Lbvh* pb = &b;  // a task would copy a reference parameter's object
+        for (int c : {b.childA[i], b.childB[i]}) {
+            if (c > 0) {
+#pragma omp task firstprivate(c, pb, level)
+                refit_subtree(*pb, c - 1, level + 1);
+            }
+        }
+#pragma omp taskwait
+        Box bx = identity_box();
+        expand(bx, child_box(b.childA[i]));
+        expand(bx, child_box(b.childB[i]));
+        b.int_box[i] = bx;
+        return;
+    }
+    std::vector<std::pair<int, char>> stack;  // {node, children pushed}
+    stack.push_back({i, 0});
+    while (!stack.empty()) {
+        auto& top = stack.back();
+        const int k = top.first;
+        if (!top.second) {
+            top.second = 1;
+            const int ca = b.childA[k], cb = b.childB[k];
+            if (cb > 0) stack.push_back({cb - 1, 0});
+            if (ca > 0) stack.push_back({ca - 1, 0});
+            continue;
+        }
+        stack.pop_back();
+        Box bx = identity_box();
+        expand(bx, child_box(b.childA[k]));
+        expand(bx, child_box(b.childB[k]));
+        b.int_box[k] = bx;
+    }
+}
+
 void build_lbvh(Lbvh& b, const float* xyz, int nv, const uint32_t* tris, int nt, float depth) {
     b.T = nt;
     b.verts.resize(nv);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nv; ++i) b.verts[i] = cvt<float>(xyz + 3 * i);
     b.tris.assign(tris, tris + 3 * (size_t)nt);
     b.tri_box.resize(nt);
@@ -207,14 +249,32 @@ void build_lbvh(Lbvh& b, const float* xyz, int nv, const uint32_t* tris, int nt,
 #pragma omp parallel for schedule(static)
     for (int t = 0; t < nt; ++t)
         b.tri_box[t] = expanded_box(b.verts[tris[3 * t]], b.verts[tris[3 * t + 1]], b.verts[tris[3 * t + 2]], depth);
+    // root box: identity U every box (fmin/fmax are exact, so per-thread partial
+    // unions merged afterwards give the same box as one pass in order)
     b.root = identity_box();
-    for (int t = 0; t < nt; ++t) expand(b.root, b.tri_box[t]);
+#pragma omp parallel
+    {
+        Box part = identity_box();
+#pragma omp for schedule(static) nowait
+        for (int t = 0; t < nt; ++t) expand(part, b.tri_box[t]);
+#pragma omp critical
+        expand(b.root, part);
+    }
 #pragma omp parallel for schedule(static)
     for (int t = 0; t < nt; ++t) b.tri_code[t] = morton3d(unitcube_pos(b.root, centroid(b.tri_box[t])));
-    // indices_sort (stable: ties by triangle index) + remove_redundant + filter
-    std::vector<int32_t> idx(nt);
+    // indices_sort (stable: ties by triangle index) + remove_redundant + filter.
+    // The stable order by code is unique; it is formed here by three stable
+    // counting passes over 10-bit digits of the 30-bit codes, least significant
+    // first (the same permutation std::stable_sort gives, in linear time).
+    std::vector<int32_t> idx(nt), tmp(nt);
     std::iota(idx.begin(), idx.end(), 0);
-    std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return b.tri_code[a] < b.tri_code[c]; });
+    for (int shift = 0; shift < 30; shift += 10) {
+        std::vector<uint32_t> count(1025, 0);
+        for (int k = 0; k < nt; ++k) ++count[((b.tri_code[idx[k]] >> shift) & 1023u) + 1];
+        for (int d = 0; d < 1024; ++d) count[d + 1] += count[d];
+        for (int k = 0; k < nt; ++k) tmp[count[(b.tri_code[idx[k]] >> shift) & 1023u]++] = idx[k];
+        idx.swap(tmp);
+    }
     b.sorted_code.clear();
     b.sorted_tri.clear();
     for (int k = 0; k < nt; ++k) {
@@ -228,6 +288,7 @@ void build_lbvh(Lbvh& b, const float* xyz, int nv, const uint32_t* tris, int nt,
     b.leaf_box.resize(n);
     b.leaf_v0.resize(n);
     b.leaf_n.resize(n);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         int t = b.sorted_tri[i];
         b.leaf_box[i] = b.tri_box[t];
@@ -242,7 +303,9 @@ void build_lbvh(Lbvh& b, const float* xyz, int nv, const uint32_t* tris, int nt,
     b.parent_leaf.assign(n, 0);
     b.int_box.assign(std::max(ni, 0), identity_box());
     const uint32_t* c = b.sorted_code.data();
-    // processInternalNode (cudaBRT.cu:120-161)
+    // processInternalNode (cudaBRT.cu:120-161); every node has one parent, so the
+    // nodes are independent
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < ni; ++i) {
         auto r = determine_range(c, ni, i);
         int split = find_split(c, r.first, r.second);
@@ -255,26 +318,11 @@ void build_lbvh(Lbvh& b, const float* xyz, int nv, const uint32_t* tris, int nt,
     }
     // calculateBoudingBox (cudaBRT.cu:166-206): internal = identity U A U B, post-order
     if (ni > 0) {
-        std::vector<int> stack;
-        std::vector<char> done(ni, 0);
-        stack.push_back(0);
-        while (!stack.empty()) {
-            int i = stack.back();
-            int ca = b.childA[i], cb = b.childB[i];
-            bool ready = true;
-            if (ca > 0 && !done[ca - 1]) { stack.push_back(ca - 1); ready = false; }
-            if (cb > 0 && !done[cb - 1]) { stack.push_back(cb - 1); ready = false; }
-            if (!ready) continue;
-            stack.pop_back();
-            Box bx = identity_box();
-            expand(bx, ca < 0 ? b.leaf_box[-ca - 1] : b.int_box[ca - 1]);
-            expand(bx, cb < 0 ? b.leaf_box[-cb - 1] : b.int_box[cb - 1]);
-            b.int_box[i] = bx;
-            done[i] = 1;
-        }
+#pragma omp parallel
+#pragma omp single
+        refit_subtree(b, 0, 0);
     }
 }
-
 // D_BVH::intersect (cudaBRT.cu:239-285): first overlapping leaf, children tested
 // pairwise, leaves before descent, left pushed before right.
 template <typename T>
@@ -425,7 +473,25 @@ struct Sim {
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < N; ++i) vertex_step(i, X, XO, Y[i], YO[i]);
         cur ^= 1;
+        // the contact set of this step (which vertices were projected, along which
+        // normal) folded into a running hash: two runs with equal hashes had equal
+        // contact sets in every step (up to a hash collision)
+        uint64_t h = contact_hash ^ (0x9e3779b97f4a7c15ull * (uint64_t)(++steps_taken));
+        for (int i = 0; i < N; ++i) {
+            if (n[i].x == 0 && n[i].y == 0 && n[i].z == 0) continue;
+            const double c[3] = {(double)n[i].x, (double)n[i].y, (double)n[i].z};
+            uint64_t w[3];
+            std::memcpy(w, c, sizeof w);
+            for (uint64_t v : {(uint64_t)i, w[0], w[1], w[2]}) {
+                h ^= v;
+                h *= 0x100000001b3ull;  // FNV-1a-style mixing over 64-bit words
+                h ^= h >> 29;
+            }
+        }
+        contact_hash = h;
     }
+    uint64_t contact_hash = 0;
+    uint64_t steps_taken = 0;
 
     // ---------------- adjoint (FP64 reference gradient) ----------------
     // One step with the contact set frozen: contact[i] >= 0 marks vertices that
@@ -639,6 +705,13 @@ void orc_sim_set_state(void* hv, const float* x, const float* xo, const float* n
             if (n) s->n[i] = cvt<TT>(n + 3 * i);
         }
     });
+}
+
+// Running hash of every step's contact set since the simulator was created.
+uint64_t orc_sim_contact_hash(void* hv) {
+    uint64_t r = 0;
+    ORC_DISPATCH(hv, r = s->contact_hash);
+    return r;
 }
 
 int orc_sim_n_leaves(void* hv) {
