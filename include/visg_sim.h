@@ -398,6 +398,14 @@ int visg_mesh_rotate(float* xyz, int32_t n, float angle_degrees, int32_t axis);
  * the device is still usable afterwards.  Takes about a second (the staging wait's
  * limit).  No counterpart in the reference. */
 int visg_selftest_bounded_waits(int32_t* gave_up);
+/* Self-test of the step's exact arithmetic: the zero-damping spring sum evaluates two
+ * springs per packed (f32x2) operation and takes each spring's length and its
+ * reciprocal from its own correctly rounded square root and reciprocal (Newton
+ * corrections of the hardware approximations) on [2^-100, 2^100), the intrinsics
+ * outside.  This runs that code on every float of the range, on the current device,
+ * against __fsqrt_rn and __frcp_rn(__fsqrt_rn(.)): *checked floats, *mismatches
+ * (must be 0).  Takes well under a second.  No counterpart in the reference. */
+int visg_selftest_exact_math(uint64_t* checked, uint64_t* mismatches);
 
 int visg_lbvh_build_noalloc(const float* d_xyz, const float* d_normals, int32_t n_vertices,
                             const uint32_t* d_tris, int32_t n_tris, float thickness, float box_depth,

@@ -52,6 +52,7 @@ def lib():
         "visg_default_params": (None, [C.POINTER(VisgParams)]),
         "visg_version": (C.c_char_p, []),
         "visg_selftest_bounded_waits": (C.c_int, [_i32p]),
+        "visg_selftest_exact_math": (C.c_int, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "visg_batch_time_kernels": (C.c_int, [_vp, C.c_int32, _fp, _fp]),
         "visg_last_error": (C.c_char_p, []),
         "visg_create": (C.c_int, [C.POINTER(VisgParams), _fp, C.c_int32, C.POINTER(_u32p), C.POINTER(_vp),
@@ -476,6 +477,14 @@ def selftest_bounded_waits() -> int:
     bits = C.c_int32()
     _check(lib().visg_selftest_bounded_waits(C.byref(bits)))
     return bits.value
+
+
+def selftest_exact_math() -> tuple[int, int]:
+    """Run visg_selftest_exact_math: the step's packed square root and reciprocal on
+    every float of their range against the CUDA intrinsics; (checked, mismatches)."""
+    n, bad = C.c_uint64(0), C.c_uint64(0)
+    _check(lib().visg_selftest_exact_math(C.byref(n), C.byref(bad)))
+    return int(n.value), int(bad.value)
 
 
 def springs_from_mesh(xyz, tris):

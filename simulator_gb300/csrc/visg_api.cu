@@ -1605,6 +1605,27 @@ int visg_selftest_bounded_waits(int32_t* gave_up) {
     return VISG_OK;
 }
 
+int visg_selftest_exact_math(uint64_t* checked, uint64_t* mismatches) {
+    ApiRange range_("visg_selftest_exact_math");
+    if (!checked || !mismatches) return fail(VISG_ERR_INVALID_ARG, "NULL output");
+    *checked = *mismatches = 0;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return fail(VISG_ERR_NO_DEVICE, "no CUDA device");
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d, 3 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(e, "self-test buffer");
+    unsigned long long h[3] = {0, 0, 0};
+    e = cudaMemset(d, 0, sizeof h);
+    if (e == cudaSuccess) e = launch_selftest_exact_math(d, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "self-test of the packed square root and reciprocal");
+    *checked = h[0];
+    *mismatches = h[1] + h[2];
+    return VISG_OK;
+}
+
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas) {
     ApiRange range_("visg_batch_autotune");
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");

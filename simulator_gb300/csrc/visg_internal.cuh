@@ -192,6 +192,8 @@ int step_max_ctas_per_sm(int variant, int block, int win_cap);
 // self-tests of the bounded waits: each must give up and set ERR_TIMEOUT in *err
 cudaError_t launch_selftest_mbar_wait(int* err, cudaStream_t s);
 cudaError_t launch_selftest_look_back(const uint32_t* zero_status, int* err, cudaStream_t s);
+// exhaustive check of the packed square root and reciprocal: cnt[3] = {checked, bad roots, bad reciprocals}
+cudaError_t launch_selftest_exact_math(unsigned long long* cnt, cudaStream_t s);
 
 // first-hit queries of external points against one body
 cudaError_t launch_query(BvhView v, const float* pts, int n, int* leaf, int* inside, float* dist,

@@ -155,6 +155,39 @@ __device__ __forceinline__ f3 spring_force(f3 x, f3 vel, float4 t0, float4 t1, f
     return mul(c, mul(dP, __frcp_rn(dist)));  // normalize(dP) = dP * (1 / |dP|)
 }
 
+// Two springs of one vertex at once, spring damping exactly +0 (spring_force<true>
+// on each spring, operation for operation).  The x and y components of a spring's
+// vectors travel as one packed pair (a record's x, y are adjacent words), z alone;
+// the two springs' scalar chains (|dP|^2, the square root and its reciprocal, the
+// rest-length term) travel as one pair.  Every packed operation rounds each lane as
+// the scalar intrinsic would, and sqrt_rcp_pair returns __fsqrt_rn / __frcp_rn's
+// bits, so each force is bit-identical to the scalar form in fewer instructions
+// (sm_100+ f32x2 arithmetic).
+__device__ __forceinline__ void spring_pair(fp2 xxy, float xz, float4 ta, float4 tb, fp2 nk, fp2 rest, fp2 eps2,
+                                            float eps, fp2& f_xy_a, float& fz_a, fp2& f_xy_b, float& fz_b) {
+    const fp2 da = add2(sub2(xxy, pk2(ta.x, ta.y)), eps2), db = add2(sub2(xxy, pk2(tb.x, tb.y)), eps2);
+    const float dza = __fadd_rn(__fsub_rn(xz, ta.z), eps), dzb = __fadd_rn(__fsub_rn(xz, tb.z), eps);
+    const fp2 qa = mul2(da, da), qb = mul2(db, db);
+    const fp2 s = pk2(__fadd_rn(__fadd_rn(lo2(qa), hi2(qa)), __fmul_rn(dza, dza)),
+                      __fadd_rn(__fadd_rn(lo2(qb), hi2(qb)), __fmul_rn(dzb, dzb)));  // dot(dP, dP)
+    fp2 dist, inv;
+    sqrt_rcp_pair(s, dist, inv);
+    const fp2 c = mul2(nk, sub2(dist, rest));  // -k (|dP| - L0)
+    const float ca = lo2(c), cb = hi2(c), ia = lo2(inv), ib = hi2(inv);
+    f_xy_a = pk2(__fmul_rn(ca, __fmul_rn(lo2(da), ia)), __fmul_rn(ca, __fmul_rn(hi2(da), ia)));
+    fz_a = __fmul_rn(ca, __fmul_rn(dza, ia));
+    f_xy_b = pk2(__fmul_rn(cb, __fmul_rn(lo2(db), ib)), __fmul_rn(cb, __fmul_rn(hi2(db), ib)));
+    fz_b = __fmul_rn(cb, __fmul_rn(dzb, ib));
+}
+
+// One 16-byte load that the compiler may not merge with an earlier load of the same
+// address (a value read again later instead of being held in registers meanwhile).
+__device__ __forceinline__ float4 ld_once(const float4* p) {
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+
 // Vertex records are read through the read-only path (about half the neighbour
 // reads hit L1: rows of a grid share most neighbours).
 struct GlobalRecords {
@@ -178,6 +211,31 @@ __device__ __forceinline__ f3 list_sum(const Rec& rec, const Ent& ep, const floa
                                        const int end, const float nk, const bool perk, f3 x, f3 vel, float kd,
                                        f3 eps3, bool drec, float dt) {
     f3 acc = mk3(0.0f, 0.0f, 0.0f);
+    if (FAST) {  // two springs per packed evaluation; the sum stays in CSR order
+        const fp2 xxy = pk2(x.x, x.y), eps2 = splat2(eps3.x), nk2 = splat2(nk);
+        fp2 axy = pk2(0.0f, 0.0f);
+        float az = 0.0f;
+        for (; e + 1 < end; e += 2) {
+            const uint2 ea = ep[e], eb = ep[e + 1];
+            const int ja = (int)(ea.x & END_MASK), jb = (int)(eb.x & END_MASK);
+            const float4 a0 = rec.r0(ja), b0 = rec.r0(jb);
+            const fp2 k2 = perk ? pk2(-__ldg(kp + 32 * e), -__ldg(kp + 32 * (e + 1))) : nk2;
+            fp2 fa, fb;
+            float fza, fzb;
+            spring_pair(xxy, x.z, a0, b0, k2, pk2(__uint_as_float(ea.y), __uint_as_float(eb.y)), eps2, eps3.x, fa, fza,
+                        fb, fzb);
+            axy = add2(add2(axy, fa), fb);
+            az = __fadd_rn(__fadd_rn(az, fza), fzb);
+        }
+        acc = mk3(lo2(axy), hi2(axy), az);
+        if (e < end) {
+            const uint2 ea = ep[e];
+            const float4 a0 = rec.r0((int)(ea.x & END_MASK));
+            const float ka = perk ? -__ldg(kp + 32 * e) : nk;
+            acc = add(acc, spring_force<true>(x, vel, a0, a0, ka, __uint_as_float(ea.y), kd, eps3, drec, dt));
+        }
+        return acc;
+    }
     for (; e + 1 < end; e += 2) {
         const uint2 ea = ep[e], eb = ep[e + 1];
         const int ja = (int)(ea.x & END_MASK), jb = (int)(eb.x & END_MASK);
@@ -249,32 +307,29 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
     const bool active = i < td.z;
     const int ii = active ? i : td.y;
     const float4 s0 = rec.r0(ii);
-    const float4 s1 = rec.r1(ii);
     const f3 x = mk3(s0.x, s0.y, s0.z);
-    const f3 rv = mk3(s0.w, s1.x, s1.y);  // v, or D = x - x_old with drec
-    const uint32_t flags = __float_as_uint(s1.z);
     const uint2 cnt = __ldg(&a.vcount[ii]);
     const bool pinned = (cnt.y & PIN_BIT) != 0u;
     f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
     bool has_n = false;
+    uint32_t flags = 0u;
+    float margin = 0.0f;
     if (active && !pinned) {
         const int lane = (int)(threadIdx.x & 31u);
         const uint32_t sb = __ldg(&a.slice_off[td.w + (int)(threadIdx.x >> 5)]) + (uint32_t)lane;  // row entry 0
-        // x - x_old: from the record (drec), else from x_old in the other buffer
-        f3 xo = x, d = rv, vel = rv;
-        if (!P.drec) {
-            if (!(flags & FLAG_XO_IS_X)) xo = xyz(a.state_out[2 * ii]);
-            d = sub(x, xo);
-        }
-        f3 np = mk3(0.0f, 0.0f, 0.0f);
-        if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
-        // force damping: with drec and damping exactly +0 the term v * +0 is a signed
-        // zero for every tame v, and g m + (+-0) only differs in the sign of a zero
-        // component, which the first list's sum (never -0) erases
+        // The zero-damping sum needs only positions: there the rest of the record
+        // (v or D, flags, the query cache's margin) is read after the sum, not held in
+        // registers across it.  With drec and force damping exactly +0 the term v * +0
+        // is a signed zero for every tame v, and g m + (+-0) only differs in the sign
+        // of a zero component, which the first list's sum (never -0) erases.
+        const bool pos_only = KD0 && P.drec && __float_as_uint(P.damp) == 0u && !wild;
+        f3 vel = mk3(0.0f, 0.0f, 0.0f);
         f3 F0 = mul(grav, P.mass);
-        if (!P.drec || __float_as_uint(P.damp) != 0u || wild) {
-            if (P.drec) vel = divs(rv, P.dt);
-            F0 = add(F0, mul(vel, P.damp));
+        if (!pos_only) {
+            const float4 s1 = rec.r1(ii);
+            const f3 rv = mk3(s0.w, s1.x, s1.y);  // v, or D = x - x_old with drec
+            vel = P.drec ? divs(rv, P.dt) : rv;
+            if (!P.drec || __float_as_uint(P.damp) != 0u || wild) F0 = add(F0, mul(vel, P.damp));
         }
         const Entries<SMEM_ENT> ep{ebase + (sb - e0)};
         const float* kp = perk ? a.sellk + sb : nullptr;
@@ -287,13 +342,26 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
             // the wild flag says when one was not) or c is not finite (then F is not
             // finite either: such rows are recomputed with the damping term).
             F = row_forces<true>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
-            if (wild || !(isfinite(F.x) && isfinite(F.y) && isfinite(F.z))) {
-                if (P.drec) vel = divs(rv, P.dt);
-                F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
-            }
         } else {
             F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
         }
+        // the record again (a second read of a line this thread has just read)
+        const float4 r0 = ld_once(a.state_in + 2 * ii), r1 = ld_once(a.state_in + 2 * ii + 1);
+        const f3 rv = mk3(r0.w, r1.x, r1.y);  // v, or D = x - x_old with drec
+        flags = __float_as_uint(r1.z);
+        margin = r1.w;
+        if (KD0 && (wild || !(isfinite(F.x) && isfinite(F.y) && isfinite(F.z)))) {
+            vel = P.drec ? divs(rv, P.dt) : rv;
+            F = row_forces<false>(rec, ep, kp, cnt, x, vel, F0, P, perk != 0, eps3);
+        }
+        // x - x_old: from the record (drec), else from x_old in the other buffer
+        f3 xo = x, d = rv;
+        if (!P.drec) {
+            if (!(flags & FLAG_XO_IS_X)) xo = xyz(a.state_out[2 * ii]);
+            d = sub(x, xo);
+        }
+        f3 np = mk3(0.0f, 0.0f, 0.0f);
+        if (flags & FLAG_HAS_NORMAL) np = xyz(a.normal[ii]);
         F = sub(F, mul(dot(np, F), np));  // inelastic response (verlet.cu:151-152)
         const f3 adt = mul(mul(divs(F, P.mass), P.dt), P.dt);
         if (refv) xn = add(sub(add(x, x), xo), adt);  // never with drec
@@ -313,7 +381,7 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
         bool query = false;
         int leaf = -1;
         if (body && active && !pinned) {
-            const float rem = P.margin ? __fsub_rd(s1.w, disp_bound(xn, x)) : 0.0f;
+            const float rem = P.margin ? __fsub_rd(margin, disp_bound(xn, x)) : 0.0f;
             if (rem > 0.0f) {
                 skin = rem;
                 if (flags & FLAG_LEAF_CACHED) {
@@ -803,6 +871,42 @@ __global__ void k_selftest_mbar_wait(int* err) {
     if (threadIdx.x == 0 && !mbar_wait(smem_addr(&bar), 0u)) atomicOr(err, ERR_TIMEOUT);
 }
 }  // namespace
+
+namespace {
+// Every float s of [2^-100, 2^100) (the range where the step takes the packed square
+// root and reciprocal) through sqrt_rcp_pair, against __fsqrt_rn(s) and
+// __frcp_rn(__fsqrt_rn(s)).  The other lane of each pair carries a different float of
+// the range (s with its low mantissa bits reversed), checked too.  cnt[0] = floats
+// checked, cnt[1] = mismatches of the root, cnt[2] = of the reciprocal.
+__global__ void k_selftest_exact_math(unsigned long long* cnt) {
+    unsigned long long n = 0, bad_q = 0, bad_r = 0;
+    const uint64_t lo = kExactLo, hi = (uint64_t)kExactLo + kExactSpan;
+    for (uint64_t u = lo + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < hi;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (uint32_t)u;
+        const uint32_t b2 = (b & 0xffff0000u) | (__brev(b) >> 16);  // same exponent, other mantissa
+        const float sa = __uint_as_float(b), sb = __uint_as_float(b2);
+        fp2 q, r;
+        sqrt_rcp_pair(pk2(sa, sb), q, r);
+        const float qa = __fsqrt_rn(sa), qb = __fsqrt_rn(sb);
+        bad_q += (__float_as_uint(lo2(q)) != __float_as_uint(qa)) + (__float_as_uint(hi2(q)) != __float_as_uint(qb));
+        bad_r += (__float_as_uint(lo2(r)) != __float_as_uint(__frcp_rn(qa))) +
+                 (__float_as_uint(hi2(r)) != __float_as_uint(__frcp_rn(qb)));
+        n += 2;
+    }
+    atomicAdd(&cnt[0], n);
+    if (bad_q) atomicAdd(&cnt[1], bad_q);
+    if (bad_r) atomicAdd(&cnt[2], bad_r);
+}
+}  // namespace
+
+cudaError_t launch_selftest_exact_math(unsigned long long* cnt, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_selftest_exact_math<<<sms * 8, 256, 0, s>>>(cnt);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_selftest_mbar_wait(int* err, cudaStream_t s) {
     k_selftest_mbar_wait<<<1, 32, 0, s>>>(err);

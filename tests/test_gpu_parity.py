@@ -712,6 +712,16 @@ def test_trajectory_matches_reference_kernels():
     assert (np.abs(rn).sum(1) > 0).sum() > 10
 
 
+def test_packed_square_root_and_reciprocal_equal_the_intrinsics_on_every_float():
+    """The zero-damping spring sum's packed square root and reciprocal (Newton
+    corrections of the hardware approximations) on all 1,677,721,600 floats of
+    [2^-100, 2^100), each in both lanes of a pair: bit-identical to __fsqrt_rn and
+    __frcp_rn(__fsqrt_rn(.)), which is what makes the packed step exact."""
+    n, bad = vs.selftest_exact_math()
+    assert n == 2 * ((227 - 27) << 23)
+    assert bad == 0
+
+
 def test_bounded_waits_give_up_and_leave_the_device_usable():
     """Failure detection without a fault: a staging-ring wait and a radix look-back
     wait that nothing completes give up (bounded), report ERR_TIMEOUT, and the
