@@ -108,15 +108,41 @@ def peak_hbm():
         return FALLBACK_HBM, "fallback"
 
 
+STEP_SOURCES = [os.path.join(ROOT, "simulator_gb300", "csrc", f)
+                for f in ("visg_step.cu", "visg_math.cuh", "visg_internal.cuh")]
+
+
+def step_kernel_build():
+    """Identity of the fused step kernel's source: the first 16 hex digits of the
+    SHA-256 of the files it is compiled from."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in STEP_SOURCES:
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
 def committed_traffic():
     """DRAM bytes of the fused step kernel per step (all its launches) from the
-    committed ncu summary."""
+    committed ncu summary, with where they come from.  The summary records the
+    kernel build it was captured on; a figure captured on another build is not
+    reported (traffic None, and the provenance says why)."""
     try:
         text = open(TRAFFIC_FILE).read()
     except OSError:
-        return None
-    m = re.search(r"traffic_bytes_per_step:\s*([0-9.eE+]+)", text)
-    return float(m.group(1)) if m else None
+        return None, {"file": os.path.relpath(TRAFFIC_FILE, ROOT), "note": "missing"}
+    fields = dict(re.findall(r"^(traffic_[a-z_]+):\s*(.+?)\s*$", text, re.M))
+    src = {"file": os.path.relpath(TRAFFIC_FILE, ROOT), "captured_on": fields.get("traffic_capture"),
+           "scale": fields.get("traffic_scale"), "kernel_build": fields.get("traffic_build"),
+           "current_build": step_kernel_build()}
+    if "traffic_bytes_per_step" not in fields:
+        src["note"] = "no figure in the summary"
+        return None, src
+    if src["kernel_build"] != src["current_build"]:
+        src["note"] = "stale: captured on another build of the step kernel, not reported"
+        return None, src
+    return float(fields["traffic_bytes_per_step"]), src
 
 
 class ClockSampler:
@@ -213,7 +239,8 @@ def cpu_baseline(items, params, seconds: float, states=None, settle: int = 0):
         s.close()
     return {"value": nv * steps / el, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
             "sample": f"the first {len(items)} garments ({nv} vertices) from the draped state, {steps} steps "
-                      f"({el:.1f} s), {threads} OpenMP threads"}
+                      f"({el:.1f} s), {threads} OpenMP threads; the rate per vertex-step of this sample stands "
+                      f"for the whole batch (extrapolated: the sample's mix of garment sizes is not the batch's)"}
 
 
 def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: int, substeps: int = 4):
@@ -315,8 +342,9 @@ def run_reference(args, rank):
         "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "vertex-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(args), "garments": args.garments, "vertices": nv,
-                   "spring_entries": ne, "triangles": nt},
+        "config": {"workload": workload_name(args), "garments": args.garments, "substeps": args.substeps,
+                   "vertices": nv, "spring_entries": ne, "triangles": nt,
+                   "timed_sample": f"the first {args.cpu_garments} garments; the rate is extrapolated to the batch"},
         "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -491,7 +519,7 @@ def main():
     achieved = alg_bytes / t_launch / 1e9
     achieved_step = alg_bytes / (ms / 1e3 / args.steps) / 1e9  # over the whole step (both kernels)
     peak, peak_kind = peak_hbm()
-    traffic = committed_traffic()
+    traffic, traffic_source = committed_traffic()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -501,9 +529,12 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
+            "value_per_frame": {"value": value / args.substeps, "unit": "vertex-frames/s",
+                                "frame": f"1e-3 s (the configurations' time step) = {args.substeps} steps"},
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": args.scaling,
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": workload_name(args), "garments": args.garments, "vertices_per_gpu": nv,
+            "config": {"workload": workload_name(args), "garments": args.garments, "substeps": args.substeps,
+                       "vertices_per_gpu": nv,
                        "vertices_all_gpus": int(nv_all),
                        "spring_entries": ne, "triangles": nt, "contacts": contacts,
                        "launch": launch,
@@ -516,7 +547,8 @@ def main():
             "plain_loop": plain,
             "batched_vs_plain": (value / plain["value"]) if plain else None,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_source,
+                         "peak_source": peak_kind,
                          "kernel": "k_step (fused integrate + springs + collision)",
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "launch_ms": k_step_ms, "achieved_over_whole_step": achieved_step},
