@@ -28,8 +28,8 @@ Reported (one JSON line, rank 0):
   cpu_baseline the CPU restatement (OpenMP) on the same garments, bounded sample
   moving_body_configs  the plain configurations whose body moves (LBVH rebuilt
               every step), over their stated durations
-  adjoint_config  500 FP64 forward steps (checkpoint every 50) + the backward
-              sweep on a 128 x 128 sheet with a stiffness per spring
+  adjoint_config  2,000 FP64 forward steps (0.5 s; checkpoint every 50) + the
+              backward sweep on a 128 x 128 sheet with a stiffness per spring
 `--impl reference` times the reference's step logic on the host cores (the
 oracle port; the reference itself is CUDA only) on the same workload.
 """
@@ -299,17 +299,20 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
 def adjoint_config(vs, scenes, torch):
     """The differentiable configuration: a 128 x 128 sheet (16,384 vertices) with a
     stiffness per spring (the three lists' k as per-entry arrays) over the 64 x 64
-    workload's sphere (radius 0.3 m, subdivision 4, centre 0.5 m below), 500 FP64
-    forward steps with a checkpoint every 50, then the backward sweep (the gradient of
-    a mean squared final-position error for every spring's stiffness and the three
-    damping scalars).  Host wall-clock around each call (both synchronise)."""
+    workload's sphere (radius 0.3 m, subdivision 4, centre 0.5 m below), its stated
+    0.5 s as 2,000 FP64 forward steps of 2.5e-4 s (4 per 1e-3 s frame, as the other
+    workloads) with a checkpoint every 50, then the backward sweep (the gradient of a
+    mean squared final-position error for every spring's stiffness and the three
+    damping scalars).  Host wall-clock around each call (both synchronise).  The
+    forward pass's frozen active set is reported: vertices projected in every 200th
+    step, and the steps that had any."""
     cloth = scenes.grid_cloth(128, 1.0, 0.0)
     body = scenes.icosphere(4, 0.3, center=(0.0, -0.5, 0.0))
-    p = scenes.physics_params(2)
+    p = scenes.physics_params(4)
     lists = [scenes.SpringList(sl.row, sl.ent, np.full(sl.n_entries, k, np.float32))
              for sl, k in zip(cloth.lists, (2000.0, 1000.0, 500.0))]
     sim = vs.Simulator(cloth.xyz, lists, body.xyz, body.tris, body.normals, params=p, pinned=cloth.pinned)
-    steps, ckpt = 500, 50
+    steps, ckpt = 2000, 50
     sim.forward(steps, ckpt)  # warm: allocations, first launches
     sim.backward(np.zeros_like(cloth.xyz))
     sim.set_state(cloth.xyz, cloth.xyz, np.zeros_like(cloth.xyz))
@@ -317,15 +320,19 @@ def adjoint_config(vs, scenes, torch):
     t0 = time.perf_counter()
     sim.forward(steps, ckpt)
     t1 = time.perf_counter()
+    active = sim.forward_contacts()
     x = sim.positions()
     target = cloth.xyz + np.float32(0.005)
     dk, ds = sim.backward((2.0 * (x - target) / len(x)).astype(np.float32))
     t2 = time.perf_counter()
     n = len(cloth.xyz)
     out = {"vertices": n, "spring_entries": int(sum(sl.n_entries for sl in lists)), "steps": steps,
-           "checkpoint_every": ckpt, "forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
-           "value": n * steps / (t2 - t0), "unit": "vertex-steps/s (forward + backward)",
-           "grad_max_abs": float(np.abs(dk).max()), "contacts": sim.count_contacts()}
+           "seconds_simulated": steps * p.dt, "checkpoint_every": ckpt, "forward_ms": (t1 - t0) * 1e3,
+           "backward_ms": (t2 - t1) * 1e3, "value": n * steps / (t2 - t0),
+           "unit": "vertex-steps/s (forward + backward)", "grad_max_abs": float(np.abs(dk).max()),
+           "grad_finite": bool(np.isfinite(dk).all()), "contacts_at_end": sim.count_contacts(),
+           "active_set_every_200_steps": [int(c) for c in active[199::200]],
+           "steps_with_contacts": int((active > 0).sum()), "max_contacts_in_a_step": int(active.max())}
     sim.close()
     return out
 

@@ -230,10 +230,15 @@ int visg_query_points(VisgSim* sim, const float* points, int32_t n,
  *   dL_dk[e]     per CSR entry, lists concatenated in order (host, total entries)
  *   dL_dscalar[3] = dL/d verlet_damping, dL/d force_damping, dL/d spring_damping.
  * Requires a symmetric spring graph (every i->j entry has a j->i entry in the
- * same list); VISG_ERR_UNSUPPORTED otherwise.  Body is held static. */
+ * same list); VISG_ERR_UNSUPPORTED otherwise.  Body is held static.  If a gradient
+ * is not finite in float (the trajectory's sensitivity overflowed) the values are
+ * written as computed and VISG_ERR_DIVERGED is returned. */
 int visg_forward(VisgSim* sim, int32_t nsteps, int32_t checkpoint_every);
 int visg_backward(VisgSim* sim, const float* dL_dx, const float* dL_dxold,
                   float* dL_dk, float* dL_dscalar);
+/* The frozen active set of the last visg_forward, as counts: counts[s] = vertices
+ * projected onto the body in forward step s, for s < n <= nsteps.  Synchronises. */
+int visg_forward_contacts(VisgSim* sim, int64_t* counts, int32_t n);
 
 /* ======================================================================== */
 /* Batched form: many garments, each with its own body; every launch covers many garments

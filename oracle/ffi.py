@@ -44,6 +44,11 @@ def lib():
         L.orc_sim_n_leaves.restype = C.c_int
         L.orc_sim_contact_hash.argtypes = [C.c_void_p]
         L.orc_sim_contact_hash.restype = C.c_uint64
+        L.orc_sim_record_contacts.argtypes = [C.c_void_p, C.c_int]
+        L.orc_sim_record_contacts.restype = C.c_void_p
+        L.orc_sim_step_forced.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        L.orc_sim_step_forced.restype = C.c_int
+        L.orc_contacts_free.argtypes = [C.c_void_p]
         L.orc_sim_export_lbvh.argtypes = [C.c_void_p, _u32p, _fp, _u32p, _i32p, _i32p, _i32p, _i32p, _i32p,
                                           _fp, _fp, _fp]
         L.orc_sim_query.argtypes = [C.c_void_p, _fp, C.c_int, _i32p, _i32p, _dp, _dp]
@@ -64,6 +69,21 @@ def ptr(a, t):
 
 def num_threads(n: int = 0) -> int:
     return lib().orc_num_threads(n)
+
+
+class ContactRecord:
+    """A contact history recorded by OracleSim.record_contacts (freed on deletion)."""
+
+    def __init__(self, h, nsteps):
+        self.h, self.nsteps = h, nsteps
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().orc_contacts_free(self.h)
+                self.h = None
+        except Exception:
+            pass
 
 
 class OracleSim:
@@ -118,6 +138,18 @@ class OracleSim:
 
     def step(self, n: int = 1):
         lib().orc_sim_step(self.h, n)
+
+    def record_contacts(self, nsteps: int) -> "ContactRecord":
+        """Step nsteps times, keeping the leaf every vertex was projected onto in every
+        step (the contact history)."""
+        return ContactRecord(lib().orc_sim_record_contacts(self.h, nsteps), nsteps)
+
+    def step_forced(self, record: "ContactRecord", first: int = 0, n: int | None = None):
+        """Replay steps [first, first + n) of a contact history instead of deciding
+        contacts: the projections of the record, by the branch's own formula."""
+        n = record.nsteps - first if n is None else n
+        if lib().orc_sim_step_forced(self.h, record.h, first, n) != 0:
+            raise RuntimeError("contact record does not fit this simulator or range")
 
     def contact_hash(self) -> int:
         """Running hash of every step's contact set (projected vertices and their

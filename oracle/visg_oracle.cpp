@@ -394,9 +394,11 @@ struct Sim {
         build_lbvh(bvh, v.data(), nv, tr.data(), (int)tr.size() / 3, p.box_depth);
     }
 
-    // collision_response_projection (verlet.cu:24-50)
-    bool collide(V3<T>& pos, V3<T>& pos_old, V3<T>& nrm) const {
+    // collision_response_projection (verlet.cu:24-50); *leaf_used = the leaf the
+    // vertex was projected onto, or -1
+    bool collide(V3<T>& pos, V3<T>& pos_old, V3<T>& nrm, int* leaf_used = nullptr) const {
         int leaf = first_hit(bvh, pos);
+        if (leaf_used) *leaf_used = -1;
         if (leaf >= 0) {
             T dist;
             V3<T> normal;
@@ -406,6 +408,7 @@ struct Sim {
                 pos = pos + dist * normal;
                 pos_old = pos;
                 nrm = normal;
+                if (leaf_used) *leaf_used = leaf;
                 return true;
             }
         }
@@ -413,11 +416,29 @@ struct Sim {
         return false;
     }
 
+    // Contact replay (a check of derivatives, not part of the reference's algorithm):
+    // when `forced` is set, the step does not decide contacts; vertex i is projected
+    // onto the plane of leaf forced[i] (or not at all for -1) by the branch's own
+    // formula x' = x* - ((x* - v0) . n) n, which for dist <= 0 is the reference's
+    // x* + |dist| n to the last bit.  `record`, when set, receives the leaf each
+    // vertex of an ordinary step was projected onto.  A forward pass replayed with
+    // another parameter value then stays on the recorded contact history, so its
+    // difference quotients are derivatives of the same piece of the trajectory that
+    // a frozen-active-set adjoint differentiates.
+    const int* forced = nullptr;
+    int* record = nullptr;
+
     // verlet kernel body (verlet.cu:129-161) for one vertex; writes outputs.
     void vertex_step(int i, const std::vector<V3<T>>& X, const std::vector<V3<T>>& XO,
                      V3<T>& xout, V3<T>& xoout) {
         V3<T> pos = X[i], pos_old = XO[i];
-        if (pinned[i]) { xout = pos; xoout = pos; n[i] = mk<T>(0, 0, 0); return; }
+        if (pinned[i]) {
+            xout = pos;
+            xoout = pos;
+            n[i] = mk<T>(0, 0, 0);
+            if (record) record[i] = -1;
+            return;
+        }
         const T dt = (T)p.dt, mass = (T)p.mass, damp = (T)p.force_damping, kd = (T)p.spring_damping;
         V3<T> vel = (pos - pos_old) / dt;
         V3<T> gravity = mk<T>((T)p.gravity[0], (T)p.gravity[1], (T)p.gravity[2]);
@@ -453,9 +474,21 @@ struct Sim {
         else
             pos = (pos + ((T)p.verlet_damping * (pos - pos_old))) + ((acc * dt) * dt);
         pos_old = tmp;
-        if (p.collide && bvh.Tp > 0) {
+        if (p.collide && bvh.Tp > 0 && forced) {
+            const int lf = forced[i];
+            if (lf >= 0) {
+                T dist;
+                V3<T> normal;
+                prim_intersect(bvh, lf, pos, dist, normal);
+                pos = pos - dist * normal;
+                pos_old = pos;
+                n[i] = normal;
+            } else {
+                n[i] = mk<T>(0, 0, 0);
+            }
+        } else if (p.collide && bvh.Tp > 0) {
             V3<T> nn;
-            collide(pos, pos_old, nn);
+            collide(pos, pos_old, nn, record ? record + i : nullptr);
             n[i] = nn;
         } else {
             n[i] = mk<T>(0, 0, 0);
@@ -706,6 +739,45 @@ void orc_sim_set_state(void* hv, const float* x, const float* xo, const float* n
         }
     });
 }
+
+// Contact record / replay (see Sim::forced): orc_sim_record_contacts steps nsteps
+// times, keeping the leaf every vertex was projected onto in every step, and
+// returns the record; orc_sim_step_forced replays steps [first, first + n) of a
+// record (on a simulator of the same cloth and body); orc_contacts_free frees it.
+struct ContactRecord {
+    int n = 0;
+    std::vector<std::vector<int>> leaf;  // per step, per vertex: leaf or -1
+};
+void* orc_sim_record_contacts(void* hv, int nsteps) {
+    auto* rec = new ContactRecord();
+    ORC_DISPATCH(hv, {
+        rec->n = s->N;
+        rec->leaf.assign(nsteps, std::vector<int>(s->N, -1));
+        for (int k = 0; k < nsteps; ++k) {
+            s->record = rec->leaf[k].data();
+            s->step();
+        }
+        s->record = nullptr;
+    });
+    return rec;
+}
+int orc_sim_step_forced(void* hv, void* recv, int first, int nsteps) {
+    auto* rec = (ContactRecord*)recv;
+    int bad = 0;
+    ORC_DISPATCH(hv, {
+        if (rec->n != s->N || first < 0 || first + nsteps > (int)rec->leaf.size()) {
+            bad = 1;
+        } else {
+            for (int k = 0; k < nsteps; ++k) {
+                s->forced = rec->leaf[first + k].data();
+                s->step();
+            }
+            s->forced = nullptr;
+        }
+    });
+    return bad ? -1 : 0;
+}
+void orc_contacts_free(void* recv) { delete (ContactRecord*)recv; }
 
 // Running hash of every step's contact set since the simulator was created.
 uint64_t orc_sim_contact_hash(void* hv) {

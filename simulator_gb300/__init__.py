@@ -77,6 +77,7 @@ def lib():
         "visg_query_points": (C.c_int, [_vp, _fp, C.c_int32, _i32p, _i32p, _fp, _fp]),
         "visg_forward": (C.c_int, [_vp, C.c_int32, C.c_int32]),
         "visg_backward": (C.c_int, [_vp, _fp, _fp, _fp, _fp]),
+        "visg_forward_contacts": (C.c_int, [_vp, C.POINTER(C.c_int64), C.c_int32]),
         "visg_batch_create": (C.c_int, [C.POINTER(VisgParams), C.POINTER(_vp)]),
         "visg_batch_add": (C.c_int, [_vp, _fp, C.c_int32, C.POINTER(_u32p), C.POINTER(_vp), C.POINTER(_fp),
                                      _u32p, C.c_int32, _fp, _fp, C.c_int32, _u32p, C.c_int32, _i32p]),
@@ -319,6 +320,13 @@ class Simulator:
     # ---- differentiation
     def forward(self, nsteps: int, checkpoint_every: int = 50):
         _check(lib().visg_forward(self.h, nsteps, checkpoint_every))
+        self._fwd_steps = nsteps
+
+    def forward_contacts(self):
+        """Vertices projected in each step of the last forward() (the frozen active set)."""
+        c = np.zeros(getattr(self, "_fwd_steps", 0), np.int64)
+        _check(lib().visg_forward_contacts(self.h, c.ctypes.data_as(C.POINTER(C.c_int64)), len(c)))
+        return c
 
     def backward(self, dL_dx, dL_dxo=None):
         dk = np.zeros(sum(self.n_entries), np.float32)

@@ -164,7 +164,7 @@ __global__ void k_step_f64(const double* __restrict__ x, const double* __restric
                            double* __restrict__ xon_out, double* __restrict__ nrm, const uint32_t* __restrict__ rowp,
                            const uint2* __restrict__ ent, const float* __restrict__ kent, const BvhView* bodies,
                            const float4* __restrict__ body_verts, const uint32_t* __restrict__ body_tris,
-                           const StepParams P, int refv, int collide, int n, int* err) {
+                           const StepParams P, int refv, int collide, int n, int* err, unsigned* contacts) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R pos0 = rld(x, i), pold = rld(xo, i);
@@ -232,6 +232,11 @@ __global__ void k_step_f64(const double* __restrict__ x, const double* __restric
     rst(xn_out, i, pos);
     rst(xon_out, i, pos_old);
     rst(nrm, i, nn);
+    if (contacts) {  // vertices projected in this step, one atomic per warp
+        const unsigned act = __activemask();
+        const unsigned m = __ballot_sync(act, nn.x != 0.0 || nn.y != 0.0 || nn.z != 0.0);
+        if (m && (int)(threadIdx.x & 31u) == __ffs(act) - 1) atomicAdd(contacts, (unsigned)__popc(m));
+    }
 }
 
 __global__ void k_widen(const float* __restrict__ src, double* __restrict__ dst, int64_t n) {
@@ -329,10 +334,10 @@ __global__ void k_adj_gather(const AdjArgs a) {
 cudaError_t launch_step_f64(const double* x, const double* xo, double* xn, double* xon, double* nrm,
                             const uint32_t* rowp, const uint2* ent, const float* kent, const BvhView* bodies,
                             const float4* body_verts, const uint32_t* body_tris, const StepParams& p, int refv,
-                            int collide, int n, int* err, cudaStream_t s) {
+                            int collide, int n, int* err, unsigned* contacts, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     k_step_f64<<<(n + 255) / 256, 256, 0, s>>>(x, xo, xn, xon, nrm, rowp, ent, kent, bodies, body_verts, body_tris, p,
-                                              refv, collide, n, err);
+                                              refv, collide, n, err, contacts);
     return cudaGetLastError();
 }
 

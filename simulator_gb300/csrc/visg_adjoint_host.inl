@@ -60,6 +60,10 @@ int Engine::forward(int nsteps, int ckpt) {
     if (!adj.G) CU(cudaMalloc((void**)&adj.G, n3 * sizeof(double)));
     if (!adj.dk) CU(cudaMalloc((void**)&adj.dk, (size_t)std::max<int64_t>(E, 1) * sizeof(double)));
     if (!adj.dsc) CU(cudaMalloc((void**)&adj.dsc, 3 * sizeof(double)));
+    if (adj.contacts) cudaFree(adj.contacts);
+    adj.contacts = nullptr;
+    CU(cudaMalloc((void**)&adj.contacts, (size_t)nsteps * sizeof(unsigned)));
+    CU(cudaMemsetAsync(adj.contacts, 0, (size_t)nsteps * sizeof(unsigned), stream));
     adj.ckpt = ckpt;
     adj.nsteps = nsteps;
     adj.ready = false;
@@ -71,7 +75,7 @@ int Engine::forward(int nsteps, int ckpt) {
     int c = 0;
     for (int s = 0; s < nsteps; ++s) {
         if (s % ckpt == 0) CU(save64(c, adj.ck[s / ckpt]));
-        CU(step64(c));
+        CU(step64(c, adj.contacts + s));
         c ^= 1;
     }
     // the simulator continues from the FP64 final state, rounded to float
@@ -84,15 +88,27 @@ int Engine::forward(int nsteps, int ckpt) {
     return VISG_OK;
 }
 
-// one FP64 step from buffer c of s64 into buffer c ^ 1 (normals in place)
-cudaError_t Engine::step64(int c) {
+// one FP64 step from buffer c of s64 into buffer c ^ 1 (normals in place); with
+// `contacts`, the step's projected vertices are counted there
+cudaError_t Engine::step64(int c, unsigned* contacts) {
     const size_t n3 = 3 * (size_t)N;
     const double* x = adj.s64 + 2 * (size_t)c * n3;
     double* y = adj.s64 + 2 * (size_t)(c ^ 1) * n3;
     const bool coll = p.collide && any_body;
     return launch_step_f64(x, x + n3, y, y + n3, adj.s64 + 4 * n3, d_rowp, d_ent, d_k, d_views,
                            coll ? bvh[0].verts : nullptr, coll ? bvh[0].tris : nullptr, step_params(),
-                           (variant() & SV_REFV) ? 1 : 0, coll ? 1 : 0, (int)N, d_err, stream);
+                           (variant() & SV_REFV) ? 1 : 0, coll ? 1 : 0, (int)N, d_err, contacts, stream);
+}
+
+// vertices projected in each step of the last forward pass
+int Engine::forward_contacts(int64_t* counts, int n) {
+    if (!adj.ready) return fail(VISG_ERR_STATE, "visg_forward_contacts needs a visg_forward first");
+    if (!counts || n < 0 || n > adj.nsteps) return fail(VISG_ERR_INVALID_ARG, "counts NULL or n out of range");
+    std::vector<unsigned> h((size_t)std::max(n, 1));
+    if (n > 0) CU(cudaMemcpyAsync(h.data(), adj.contacts, (size_t)n * sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    if (int r = sync()) return r;
+    for (int k = 0; k < n; ++k) counts[k] = (int64_t)h[k];
+    return VISG_OK;
 }
 
 // [x | xo | n] of FP64 buffer c into dst (9N doubles)
@@ -166,9 +182,16 @@ int Engine::backward(const float* dL_dx, const float* dL_dxo, float* dL_dk, floa
     CU(cudaMemcpyAsync(dkm.data(), adj.dk, (size_t)E * sizeof(double), cudaMemcpyDeviceToHost, stream));
     CU(cudaMemcpyAsync(dsc, adj.dsc, sizeof dsc, cudaMemcpyDeviceToHost, stream));
     if (int r = sync()) return r;
+    bool finite = std::isfinite((float)dsc[0]) && std::isfinite((float)dsc[1]) && std::isfinite((float)dsc[2]);
+    for (int64_t c = 0; c < E && finite; ++c) finite = std::isfinite((float)dkm[c]);
     if (dL_dk)
         for (int64_t c = 0; c < E; ++c) dL_dk[merged_pos[c]] = (float)dkm[c];
     if (dL_dscalar)
         for (int k = 0; k < 3; ++k) dL_dscalar[k] = (float)dsc[k];
+    if (!finite)
+        return fail(VISG_ERR_DIVERGED,
+                    "the gradient is not finite in float: the trajectory's sensitivity overflowed (an unstable "
+                    "forward, or a long stretch of sustained contact at a step size where a projected vertex's "
+                    "update amplifies perturbations); the values were written as computed");
     return VISG_OK;
 }

@@ -8,6 +8,8 @@
 // an internal stream (two graphs, one per ping-pong parity).
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include <algorithm>
 #include <cstdlib>
 #include <cstdio>
@@ -178,6 +180,7 @@ struct Engine {
         double* dk = nullptr;        // per merged entry
         double* dsc = nullptr;       // 3
         uint32_t* rev = nullptr;     // reverse entry of every merged entry
+        unsigned* contacts = nullptr;  // vertices projected in each forward step
         bool ready = false;
     } adj;
 
@@ -235,7 +238,7 @@ struct Engine {
     void free_adjoint() {
         for (auto* q : adj.ck) cudaFree(q);
         adj.ck.clear();
-        void* ps[] = {adj.s64, adj.rec, adj.lam, adj.G, adj.dk, adj.dsc, adj.rev};
+        void* ps[] = {adj.s64, adj.rec, adj.lam, adj.G, adj.dk, adj.dsc, adj.rev, adj.contacts};
         for (void* q : ps)
             if (q) cudaFree(q);
         adj = Adj();
@@ -1235,7 +1238,8 @@ struct Engine {
 
     int forward(int nsteps, int ckpt);
     int backward(const float* dL_dx, const float* dL_dxo, float* dL_dk, float* dL_dscalar);
-    cudaError_t step64(int c);
+    int forward_contacts(int64_t* counts, int n);
+    cudaError_t step64(int c, unsigned* contacts = nullptr);
     cudaError_t save64(int c, double* dst);
     cudaError_t load64(const double* src);
 };
@@ -1465,6 +1469,11 @@ int visg_forward(VisgSim* sim, int32_t nsteps, int32_t ckpt) {
     ApiRange range_("visg_forward");
     if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
     return sim->eng.forward(nsteps, ckpt);
+}
+
+int visg_forward_contacts(VisgSim* sim, int64_t* counts, int32_t n) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.forward_contacts(counts, n);
 }
 
 int visg_backward(VisgSim* sim, const float* dL_dx, const float* dL_dxo, float* dL_dk, float* dL_dscalar) {

@@ -256,7 +256,7 @@ cudaError_t launch_adjoint_step(const AdjArgs& a, cudaStream_t s);
 cudaError_t launch_step_f64(const double* x, const double* xo, double* xn, double* xon, double* nrm,
                             const uint32_t* rowp, const uint2* ent, const float* kent, const BvhView* bodies,
                             const float4* body_verts, const uint32_t* body_tris, const StepParams& p, int refv,
-                            int collide, int n, int* err, cudaStream_t s);
+                            int collide, int n, int* err, unsigned* contacts, cudaStream_t s);
 cudaError_t launch_widen(const float* src, double* dst, int64_t n, cudaStream_t s);
 cudaError_t launch_narrow(const double* src, float* dst, int64_t n, cudaStream_t s);
 

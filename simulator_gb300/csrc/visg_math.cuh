@@ -96,14 +96,13 @@ __device__ __forceinline__ fp2 splat2(float v) { return pk2(v, v); }
 // For s in [2^-100, 2^100):  q = RN(sqrt(s))  and  r = RN(1 / q), bit for bit what
 // __fsqrt_rn(s) and __frcp_rn(__fsqrt_rn(s)) return (checked against them on every
 // float of that range by visg_selftest_exact_math).  Method: Markstein's correction
-// of a hardware approximation by Newton steps whose residuals an FMA computes
-// exactly (P. W. Markstein, "Computation of elementary functions on the IBM RISC
+// of a hardware approximation by one Newton step whose residual an FMA forms with a
+// single rounding (P. W. Markstein, "Computation of elementary functions on the IBM RISC
 // System/6000 processor", IBM J. Res. Develop. 34(1), 1990; the square-root form is
 // the one of M. Cornea, J. Harrison, P. T. P. Tang, "Scientific Computing on
 // Itanium-based Systems", Intel Press, 2002, ch. 8):
-//   y ~ 1/sqrt(s) (rsqrt.approx), g = s y, h = y/2;  r = 1/2 - g h;  g += g r;  h += h r;
-//   d = s - g^2 (exact);  q = g + d h.
-//   z ~ 1/q (rcp.approx);  e = 1 - q z (exact);  r = z + z e.
+//   y ~ 1/sqrt(s) (rsqrt.approx), g = s y, h = y/2;  d = s - g^2 (one FMA);  q = g + d h.
+//   z ~ 1/q (rcp.approx);  e = 1 - q z (one FMA);  r = z + z e.
 // Lanes outside the range take the intrinsics.  (Below 2^-100 the remainder s - g^2
 // can fall among the subnormals and lose the bits the last correction needs.)
 constexpr uint32_t kExactLo = 27u << 23;                     // 2^-100
@@ -125,12 +124,9 @@ __device__ __forceinline__ void sqrt_rcp_pair(fp2 s, fp2& q, fp2& r) {
     const float sa = lo2(s), sb = hi2(s);
     if (exact_fast_domain(sa) && exact_fast_domain(sb)) {
         const fp2 y = pk2(rsqrt_approx(sa), rsqrt_approx(sb));
-        fp2 nh = mul2(y, splat2(-0.5f));  // -h
-        fp2 g = mul2(s, y);
-        const fp2 t = fma2(g, nh, splat2(0.5f));  // 1/2 - g h
-        g = fma2(g, t, g);
-        nh = fma2(nh, t, nh);
-        const fp2 dn = fma2(g, g, mul2(s, splat2(-1.0f)));  // g^2 - s, exact
+        const fp2 nh = mul2(y, splat2(-0.5f));  // -h
+        const fp2 g = mul2(s, y);
+        const fp2 dn = fma2(g, g, mul2(s, splat2(-1.0f)));  // g^2 - s
         q = fma2(dn, nh, g);                                // g + (s - g^2) h
         const fp2 nq = mul2(q, splat2(-1.0f));
         fp2 z = pk2(rcp_approx(lo2(q)), rcp_approx(hi2(q)));
