@@ -1,6 +1,9 @@
 """Garment shards across ranks: the contiguous partition by vertex count, and the rank
 group's barrier / max / sum / gather run as two gloo ranks on the host (between GPUs
-the same calls run over NCCL).  Nothing here touches a GPU."""
+the same calls run over NCCL).  The GPU test runs two ranks that each step their
+shard of a batch with the library (both on the one GPU a test run has: the ranks'
+kernels never wait on each other, and the collectives are gloo's, on the host) and
+gathers their positions to rank 0."""
 import os
 import socket
 
@@ -76,3 +79,65 @@ def test_two_gloo_ranks():
     assert out[1][3] is None
     expect = np.concatenate([np.full((w, 3), k, np.float32) for k, w in enumerate(WEIGHTS)])
     assert np.array_equal(out[0][3], expect)  # every garment's rows, in garment order
+
+
+def _rank_step(rank, world, port, q, n_garments, steps):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import torch
+    import simulator_gb300 as vs
+    from simulator_gb300 import scenes
+    from simulator_gb300.shards import RankGroup, my_shard
+    torch.cuda.set_device(0)
+    g = RankGroup("gloo")
+    items = scenes.garment_batch(n_garments, seed=3, side_range=(16, 48), subdiv_range=(2, 3),
+                                 radius_range=(0.3, 0.3), centre_depth=0.31)
+    lo, hi = my_shard([len(c.xyz) for c, _ in items], rank, world)
+    b = vs.BatchSimulator(scenes.physics_params(4))
+    for cloth, body in items[lo:hi]:
+        b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+    b.finalize()
+    b.step(steps)
+    local = b.positions()
+    contacts = g.sum(b.count_contacts())
+    b.close()
+    rows = g.gather_rows(local, dst=0)
+    q.put((rank, (lo, hi), contacts, rows))
+    g.close()
+
+
+@pytest.mark.gpu
+def test_two_ranks_step_their_shards():
+    """Six garments in two shards stepped by two ranks (400 steps; each sheet starts
+    1 cm above its sphere and lands on it): rank 0's gathered positions equal one
+    process stepping all six, bit for bit."""
+    import torch.multiprocessing as mp
+    import simulator_gb300 as vs
+    from simulator_gb300 import scenes
+    n_garments, steps = 6, 400
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_step, args=(r, 2, port, q, n_garments, steps)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = {}
+    for _ in procs:
+        rank, shard, contacts, rows = q.get(timeout=300)
+        out[rank] = (shard, contacts, rows)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert out[0][0][1] == out[1][0][0] and 0 < out[0][0][1] < n_garments  # both shards hold garments
+    items = scenes.garment_batch(n_garments, seed=3, side_range=(16, 48), subdiv_range=(2, 3),
+                                 radius_range=(0.3, 0.3), centre_depth=0.31)
+    b = vs.BatchSimulator(scenes.physics_params(4))
+    for cloth, body in items:
+        b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+    b.finalize()
+    b.step(steps)
+    whole = b.positions()
+    contacts = b.count_contacts()
+    b.close()
+    assert out[1][2] is None
+    assert np.array_equal(out[0][2], whole)
+    assert out[0][1] == out[1][1] == contacts > 0
