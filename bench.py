@@ -28,6 +28,8 @@ Reported (one JSON line, rank 0):
   cpu_baseline the CPU restatement (OpenMP) on the same garments, bounded sample
   moving_body_configs  the plain configurations whose body moves (LBVH rebuilt
               every step), over their stated durations
+  config0_plain  the 64 x 64 sheet over its sphere for its 200 frames, on the GPU
+              and, beside it, the CPU restatement on the host cores
   adjoint_config  2,000 FP64 forward steps (0.5 s; checkpoint every 50) + the
               backward sweep on a 128 x 128 sheet with a stiffness per spring
 `--impl reference` times the reference's step logic on the host cores (the
@@ -75,6 +77,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable (adjoint) config")
     ap.add_argument("--moving-only", action="store_true",
                     help="only the moving-body plain configs (one JSON object; for profiling the LBVH rebuild)")
+    ap.add_argument("--rebuilds", type=int, default=0,
+                    help="only N LBVH rebuilds of the noisy sphere's body, timed (one JSON object; profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--launch", default=None, help="block,ctas_per_sm instead of autotuning (profiling runs)")
@@ -243,6 +247,50 @@ def cpu_baseline(items, params, seconds: float, states=None, settle: int = 0):
                       f"for the whole batch (extrapolated: the sample's mix of garment sizes is not the batch's)"}
 
 
+def config0_plain(vs, scenes, torch, params, stream, substeps: int, cpu: bool):
+    """The smallest plain workload: a 64 x 64 sheet (1 m, two corners pinned) over an
+    icosphere of subdivision 4 (radius 0.3 m) centred 0.5 m below, its stated 200
+    frames (`substeps` steps each) from the initial state.  The GPU runs them as one
+    simulate call (graph replay; CUDA events on the launching stream), then again
+    from the same initial state for a second timing; with `cpu`, the oracle (float,
+    OpenMP) runs the same steps on the host cores for the CPU row beside it."""
+    cloth, body = scenes.sheet_over_sphere(64, 4)
+    n, steps = len(cloth.xyz), 200 * substeps
+    sim = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
+                       pinned=cloth.pinned)
+    sim.set_stream(stream.cuda_stream)
+    zero = np.zeros_like(cloth.xyz)
+    sim.simulate(steps)  # warm: graph capture, first launches
+    times = []
+    for _ in range(2):
+        sim.set_state(cloth.xyz, cloth.xyz, zero)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.simulate(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = min(times)
+    out = {"vertices": n, "spring_entries": int(sum(sl.n_entries for sl in cloth.lists)),
+           "triangles": int(len(body.tris)), "frames": 200, "steps": steps,
+           "gpu": {"value": n * steps / (ms / 1e3), "unit": "vertex-steps/s", "ms_per_step": ms / steps,
+                   "how": "one simulate call of all steps (graph replay), best of 2 from the initial state"},
+           "contacts_at_end": sim.count_contacts()}
+    sim.close()
+    if cpu:
+        from oracle.ffi import OracleSim, num_threads
+        o = OracleSim(params, cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, prec=4,
+                      pinned=cloth.pinned)
+        t0 = time.perf_counter()
+        o.step(steps)
+        el = time.perf_counter() - t0
+        o.close()
+        out["cpu"] = {"value": n * steps / el, "unit": "vertex-steps/s", "cores": num_threads(0), "kind": "port",
+                      "seconds": el, "sample": "the same steps from the same initial state"}
+    return out
+
+
 def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: int, substeps: int = 4):
     """The plain single-garment workloads whose body moves (LBVH rebuilt every step),
     each over its stated duration (1,000 frames for the capsules, 500 for the sphere,
@@ -293,6 +341,37 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
                      "contacts_at_end": contacts}
         del d_frames
         sim.close()
+    return out
+
+
+def rebuilds_only(vs, scenes, torch, params, n: int):
+    """The LBVH rebuild alone: the 327,680-triangle noisy sphere moved along its
+    1 Hz oscillation and rebuilt `n` times (update_body_device with positions already
+    on the device), after 3 untimed rebuilds; CUDA events around the n calls.  The
+    launches are the creation's build, 3 warm-up builds, then the n timed ones."""
+    cloth, body, motion = scenes.sheet_over_noisy_sphere(0)
+    sim = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
+                       pinned=cloth.pinned)
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    total = 3 + n
+    offs = np.stack([motion((k + 1) * params.dt) for k in range(total)]).astype(np.float32)
+    d_base = torch.from_numpy(np.ascontiguousarray(body.xyz, np.float32)).cuda()
+    d_frames = (d_base[None] + torch.from_numpy(offs).cuda()[:, None, :]).contiguous()
+    d_nrm = torch.from_numpy(np.ascontiguousarray(body.normals, np.float32)).cuda()
+    fb = d_frames.element_size() * d_base.numel()
+    for j in range(3):
+        sim.update_body_device(d_frames.data_ptr() + j * fb, d_nrm.data_ptr())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for j in range(3, total):
+        sim.update_body_device(d_frames.data_ptr() + j * fb, d_nrm.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out = {"triangles": int(len(body.tris)), "rebuilds": n, "ms_per_rebuild": e0.elapsed_time(e1) / n,
+           "leaves": sim.info()["n_leaves"]}
+    sim.close()
     return out
 
 
@@ -382,6 +461,9 @@ def main():
     sampler = ClockSampler(phys)
 
     params = scenes.physics_params(args.substeps)
+    if args.rebuilds:
+        print(json.dumps({"lbvh_rebuilds": rebuilds_only(vs, scenes, torch, params, args.rebuilds)}), flush=True)
+        return 0
     if args.moving_only:
         out = moving_body_configs(vs, scenes, torch, params, torch.cuda.current_stream(), args.steps, args.warmup,
                                   args.substeps)
@@ -509,9 +591,10 @@ def main():
                  "how": "each garment its own Simulator, stepped K steps (graph replay) one garment after another"}
         for s in sims:
             s.close()
-    moving = None
+    moving = config0 = None
     if rank == 0 and not args.no_moving:
         moving = moving_body_configs(vs, scenes, torch, params, stream, 100, 10, args.substeps)
+        config0 = config0_plain(vs, scenes, torch, params, stream, args.substeps, cpu=world == 1 and not args.no_cpu)
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_config(vs, scenes, torch)
@@ -563,6 +646,7 @@ def main():
                           "how": "one chain, CUDA events around each launch, mean of 10"},
             "cpu_baseline": cpu,
             "moving_body_configs": moving,
+            "config0_plain": config0,
             "adjoint_config": adjoint,
             "clocks": clocks,
             "gpu_launches": args.steps * launch["kernels_per_step"],

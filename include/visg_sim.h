@@ -124,11 +124,14 @@ int visg_step(VisgSim* sim, int32_t nsteps);
 
 /* New (the reference has no moving body): upload new body vertex positions (and
  * normals, for the thickness push) and rebuild the LBVH on the device:
- * expanded boxes -> root box -> Morton codes -> radix sort -> de-duplication ->
+ * expanded boxes -> root box -> Morton codes -> sort (the codes that changed since
+ * the last build merged into its order, or a radix sort) -> de-duplication ->
  * radix-tree build and refit (bvh.cu:154-297, cudaBRT.cu:120-206). */
 int visg_update_body(VisgSim* sim, const float* body_xyz, const float* body_normals);
 
-/* Same with the vertices already in device memory (n_body_vertices*3 floats). */
+/* Same with the vertices already in device memory (n_body_vertices*3 floats), read
+ * by the rebuild in stream order: the arrays must stay valid until the library's
+ * stream has run it. */
 int visg_update_body_device(VisgSim* sim, const float* d_body_xyz, const float* d_body_normals);
 
 /* Replaces Simulator::update_vertex (simulation.cu:253-257): sets x and x_old of
@@ -396,12 +399,14 @@ int visg_mesh_rotate(float* xyz, int32_t n, float angle_degrees, int32_t axis);
 #define VISG_NOALLOC_SCRATCH_BYTES (9u * 1024u * 1024u)
 /* Self-test of the device-side failure detection: runs, on the current device, one
  * kernel that waits on an mbarrier phase nothing completes (the wait of the step's
- * shared-memory staging ring) and one that looks back at a radix-sort status word
- * nothing publishes (the wait of the LBVH's radix passes and de-duplication).  Each
- * wait is bounded and must give up, record the timeout and return; *gave_up gets
- * bit 0 for the first, bit 1 for the second (3 = both behaved).  Returns VISG_OK when
- * the device is still usable afterwards.  Takes about a second (the staging wait's
- * limit).  No counterpart in the reference. */
+ * shared-memory staging ring), one that looks back at a radix-sort status word
+ * nothing publishes (the wait of the LBVH's radix passes), and one that waits at a
+ * grid barrier for CTAs that never arrive (the wait between the LBVH build's
+ * phases).  Each wait is bounded and must give up, record the timeout and return;
+ * *gave_up gets bit 0 for the first, bit 1 for the second, bit 2 for the third
+ * (7 = all behaved).  Returns VISG_OK when the device is still usable afterwards.
+ * Takes about two seconds (the staging wait's and the grid barrier's limits).  No
+ * counterpart in the reference. */
 int visg_selftest_bounded_waits(int32_t* gave_up);
 /* Self-test of the step's exact arithmetic: the zero-damping spring sum evaluates two
  * springs per packed (f32x2) operation and takes each spring's length and its

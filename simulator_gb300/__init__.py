@@ -480,8 +480,9 @@ class BatchSimulator:
 
 def selftest_bounded_waits() -> int:
     """Run the device-side failure-detection self-test (visg_selftest_bounded_waits):
-    a staging-ring wait and a radix look-back wait that nothing completes must both
-    give up and report it.  Returns the bits of the waits that gave up (3 = both)."""
+    a staging-ring wait, a radix look-back wait and an LBVH grid-barrier wait that
+    nothing completes must all give up and report it.  Returns the bits of the waits
+    that gave up (7 = all three)."""
     bits = C.c_int32()
     _check(lib().visg_selftest_bounded_waits(C.byref(bits)))
     return bits.value

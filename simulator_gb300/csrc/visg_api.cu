@@ -167,7 +167,6 @@ struct Engine {
     int64_t steps_since_check = 0;
     cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
     int chunk_steps = 16;
-    std::vector<cudaGraphExec_t> body_exec;
     int sm_count = 0;
     // adjoint records
     struct Adj {
@@ -227,11 +226,6 @@ struct Engine {
             if (chunk_exec[c]) {
                 cudaGraphExecDestroy(chunk_exec[c]);
                 chunk_exec[c] = nullptr;
-            }
-        for (auto& g : body_exec)
-            if (g) {
-                cudaGraphExecDestroy(g);
-                g = nullptr;
             }
     }
 
@@ -482,7 +476,6 @@ struct Engine {
         for (int g = 0; g < G; ++g)
             views[g] = gin[g].nt > 0 ? bvh[g].view() : BvhView{nullptr, nullptr, nullptr};
         CU(cudaMemcpy(d_views, views.data(), G * sizeof(BvhView), cudaMemcpyHostToDevice));
-        body_exec.assign(G, nullptr);
         for (int g = 0; g < G; ++g) {
             if (gin[g].nt == 0) continue;
             CU(cudaMemcpy(bvh[g].xyz_in, gin[g].bxyz.data(), gin[g].bxyz.size() * 4, cudaMemcpyHostToDevice));
@@ -713,29 +706,6 @@ struct Engine {
         return VISG_OK;
     }
 
-    int body_build(int g) {
-        if (p.use_graph) {
-            if (!body_exec[g]) {
-                cudaGraph_t gr = nullptr;
-                CU(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-                cudaError_t le = lbvh_build(bvh[g], p.thickness, p.box_depth, d_err, cap);
-                cudaError_t ee = cudaStreamEndCapture(cap, &gr);
-                if (le != cudaSuccess) {
-                    if (gr) cudaGraphDestroy(gr);
-                    return cuda_fail(le, "LBVH capture");
-                }
-                CU(ee);
-                cudaError_t ie = cudaGraphInstantiate(&body_exec[g], gr, 0);
-                cudaGraphDestroy(gr);
-                CU(ie);
-            }
-            CU(cudaGraphLaunch(body_exec[g], stream));
-        } else {
-            CU(lbvh_build(bvh[g], p.thickness, p.box_depth, d_err, stream));
-        }
-        return VISG_OK;
-    }
-
     int update_body(int g, const float* xyz, const float* nrm, cudaMemcpyKind kind) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         if (g < 0 || g >= G) return fail(VISG_ERR_INVALID_ARG, "garment out of range");
@@ -743,10 +713,17 @@ struct Engine {
         if (!xyz) return fail(VISG_ERR_INVALID_ARG, "body_xyz is NULL");
         if ((nrm != nullptr) != bvh[g].has_normals)
             return fail(VISG_ERR_INVALID_ARG, "body normals must be given iff they were given at creation");
-        CU(cudaMemcpyAsync(bvh[g].xyz_in, xyz, (size_t)bvh[g].nv * 12, kind, stream));
-        if (nrm) CU(cudaMemcpyAsync(bvh[g].nrm_in, nrm, (size_t)bvh[g].nv * 12, kind, stream));
-        CU(launch_clear_margin(d_state[cur], voff[g], voff[g + 1], stream));  // the body moves
-        return body_build(g);
+        // device arrays are read by the build itself, in stream order; host arrays are
+        // staged first.  The build also voids the garment's query-cache margins (the
+        // body moves)
+        const bool dev = kind == cudaMemcpyDeviceToDevice;
+        if (!dev) {
+            CU(cudaMemcpyAsync(bvh[g].xyz_in, xyz, (size_t)bvh[g].nv * 12, kind, stream));
+            if (nrm) CU(cudaMemcpyAsync(bvh[g].nrm_in, nrm, (size_t)bvh[g].nv * 12, kind, stream));
+        }
+        CU(lbvh_build(bvh[g], p.thickness, p.box_depth, d_err, stream, dev ? xyz : nullptr, dev ? nrm : nullptr,
+                      d_state[cur], voff[g], voff[g + 1]));
+        return VISG_OK;
     }
 
     int check_vertex(int g, uint32_t idx, int64_t* v) {
@@ -1596,21 +1573,24 @@ int visg_selftest_bounded_waits(int32_t* gave_up) {
     *gave_up = 0;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return fail(VISG_ERR_NO_DEVICE, "no CUDA device");
-    int* d = nullptr;  // [0] mbarrier wait's error word, [1] look-back's, [2] a status word nothing publishes
-    cudaError_t e = cudaMalloc((void**)&d, 16);
+    // [0] mbarrier wait's error word, [1] look-back's, [2] a status word nothing publishes,
+    // [3] grid barrier's error word, [4] an arrival counter no other CTA increments
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d, 32);
     if (e != cudaSuccess) return cuda_fail(e, "self-test buffer");
-    int h[2] = {0, 0};
-    e = cudaMemset(d, 0, 16);
+    int h[4] = {0, 0, 0, 0};
+    e = cudaMemset(d, 0, 32);
     if (e == cudaSuccess) e = launch_selftest_mbar_wait(d, nullptr);
     if (e == cudaSuccess) e = launch_selftest_look_back(reinterpret_cast<const uint32_t*>(d + 2), d + 1, nullptr);
+    if (e == cudaSuccess) e = launch_selftest_grid_wait(reinterpret_cast<uint32_t*>(d + 4), d + 3, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
-    // the device must still work after both waits gave up
-    if (e == cudaSuccess) e = cudaMemset(d, 0, 16);
+    // the device must still work after the waits gave up
+    if (e == cudaSuccess) e = cudaMemset(d, 0, 32);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     cudaFree(d);
     if (e != cudaSuccess) return cuda_fail(e, "self-test of the bounded waits");
-    *gave_up = ((h[0] & ERR_TIMEOUT) ? 1 : 0) | ((h[1] & ERR_TIMEOUT) ? 2 : 0);
+    *gave_up = ((h[0] & ERR_TIMEOUT) ? 1 : 0) | ((h[1] & ERR_TIMEOUT) ? 2 : 0) | ((h[3] & ERR_TIMEOUT) ? 4 : 0);
     return VISG_OK;
 }
 

@@ -69,10 +69,11 @@ struct __align__(16) BvhRoot {
     int root;      // root internal node, -1 when there are fewer than two leaves
     int n_leaves;  // T' (after de-duplication)
     int n_tris;    // T
-    int perm_valid;  // the sort buffers hold the last build's sorted codes and permutation
+    int perm_valid;  // codes and keys/vals[sorted] hold the last build's codes and sorted list
     float4 frame_lo, frame_hi;  // Morton frame: identity box U every expanded triangle box
     float4 top_lo, top_hi;      // box of the root node (identity U children), or of the only leaf
-    uint32_t acc[8];            // order-preserving accumulators of the frame (min xyz, max xyz)
+    int sorted;                 // which of the two sort buffers holds the last build's list
+    int pad_[3];
 };
 
 // device view of one body's LBVH, as the step and query kernels use it
@@ -98,7 +99,7 @@ struct BvhBuffers {
     int nv = 0, nt = 0;        // body vertices, triangles
     int tiles_sort = 0;        // look-back tiles of one radix pass
     bool has_normals = false;
-    bool coherent = false;     // reuse the last build's order when the codes still sort the same
+    bool coherent = false;     // merge the changed codes into the last build's sorted list
     float* xyz_in = nullptr;   // nv*3 staging (upload target)
     float* nrm_in = nullptr;   // nv*3 staging
     float4* verts = nullptr;   // nv, thickness push applied
@@ -126,16 +127,29 @@ struct BvhBuffers {
     int chunks = 0;              // chunks of nt leaves
     int lev_off[4] = {0, 0, 0, 0};
     BvhRoot* root = nullptr;
-    uint32_t* scratch = nullptr; // zeroed before every build (histograms, status words)
+    uint32_t* scratch = nullptr; // radix histograms, look-back status words, tile counters (the build clears them)
     size_t scratch_words = 0;
+    int max_ctas = 0;            // CTAs a build launches at most (one per 512 triangles)
+    float* part = nullptr;       // 8 per CTA: the CTA's box union
+    uint32_t* ucnt = nullptr;    // per CTA: distinct codes in its slice
+    uint32_t* chg = nullptr;     // count + the triangles whose code changed since the last build
+    uint32_t* sync = nullptr;    // grid-barrier counters, zero between builds
+    uint32_t* gdone = nullptr;   // per summary entry above level 0: members finished
+    int n_entries = 0;           // summary entries of all levels
 
     void plan(Arena& a, int nv_, int nt_, bool normals);
     BvhView view() const { return BvhView{nodes, leaves, root}; }
 };
 
-// Launch the full device build: vertex push -> boxes + frame -> Morton codes + digit
-// histograms -> 4 radix passes -> de-duplication -> bottom-up build + refit.
-cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s);
+// The full device build in one cooperative launch: vertex push -> boxes + frame ->
+// Morton codes -> sort (merge of the changed codes, or 4 radix passes) ->
+// de-duplication -> bottom-up build + refit.  The body's vertices (and normals) are
+// read from xyz / nrm when given (device memory, read in stream order), else from
+// the staging buffers; with margin_state, the same launch voids the query-cache
+// margins of cloth vertices [m0, m1).
+cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s,
+                       const float* xyz = nullptr, const float* nrm = nullptr, float4* margin_state = nullptr,
+                       int64_t m0 = 0, int64_t m1 = 0);
 
 // ---- step kernel arguments ---------------------------------------------------------------
 struct StepParams {
@@ -192,6 +206,7 @@ int step_max_ctas_per_sm(int variant, int block, int win_cap);
 // self-tests of the bounded waits: each must give up and set ERR_TIMEOUT in *err
 cudaError_t launch_selftest_mbar_wait(int* err, cudaStream_t s);
 cudaError_t launch_selftest_look_back(const uint32_t* zero_status, int* err, cudaStream_t s);
+cudaError_t launch_selftest_grid_wait(uint32_t* zero_counter, int* err, cudaStream_t s);
 // exhaustive check of the packed square root and reciprocal: cnt[3] = {checked, bad roots, bad reciprocals}
 cudaError_t launch_selftest_exact_math(unsigned long long* cnt, cudaStream_t s);
 

@@ -1,43 +1,54 @@
-// visg_lbvh.cu — per-step body LBVH build on the device.
+// visg_lbvh.cu — per-step body LBVH build on the device, in one launch.
 //
 // Reference (BVHAccel, src/bvh/bvh.cu:154-297; cudaBRT.cu:9-206) builds once per
 // body with a device->host->device round trip: expanded boxes and Morton codes on
 // the GPU, std::sort + duplicate removal on the CPU, then Karras internal nodes and
-// an atomic-counter refit on the GPU.  Here the whole build stays on the device,
-// in up to ten stream-ordered kernels, so it can run every step and be captured in a
-// CUDA graph:
-//   k_body_prep   vertex_extend (Mesh.cpp:101-117): v += thickness * n
-//   k_tri_boxes   expanded triangle boxes (primitive.cu:79-91) + the Morton frame
-//                 (identity box U all boxes) by warp-shuffle min/max reduction
-//   k_morton      Morton code of each box centroid in the frame (bvh.cu:20-41,71-79;
-//                 bbox.h:97-127) + the digit histograms of all four radix passes
-//   k_coherence   (bodies rebuilt every step) is the last build's permutation still
-//                 the stable order of the new codes?  Then the radix passes exit at
-//                 once; if every code is unchanged too, so does k_unique
-//   k_sort_pass   x4: stable LSD radix pass, 8-bit digits, decoupled look-back
-//                 (ties keep triangle order, i.e. sort by (code, triangle))
-//   k_unique      keep the first triangle of every distinct code
-//                 (remove_redundant, Utilities.h:35-55), look-back compaction
-//   k_build       bottom-up radix-tree build fused with the refit, per chunk of 512
-//                 sorted leaves: each leaf thread climbs with handshakes in shared
-//                 memory while both children lie in the chunk; the parent of range
-//                 [l, r] is the boundary with the longer common prefix (delta(l-1,l)
-//                 vs delta(r,r+1), delta = clz(a ^ b) as cudaBRT.cu:9-19), the second
-//                 child to arrive merges both boxes into the identity box
-//                 (calculateBoudingBox, cudaBRT.cu:166-206) and continues.  Each chunk
-//                 then publishes a summary for the nodes that span chunks
-//   k_build_top   one warp per node that spans chunks: its range ends are the nearest
-//                 boundaries with a smaller delta, its box the union of its leaves'
-//                 boxes, both read off the chunk summaries
-//                 Nodes are numbered by their split position; the tree is the same
-//                 binary radix tree processInternalNode (cudaBRT.cu:120-161) builds,
-//                 and visg_export_lbvh renumbers it into the reference's layout.
-// Every wait is bounded; a wait that gives up sets ERR_TIMEOUT and the host reports
+// an atomic-counter refit on the GPU.  Here the whole build is one cooperative
+// launch of k_rebuild, so it can run every step: persistent CTAs, all resident at
+// once, walk its phases, and a grid barrier (every CTA arrives on a counter, then
+// waits for the others, bounded) separates phases that read what others wrote:
+//   verts   vertex_extend (Mesh.cpp:101-117) v += thickness * n, stored as float4
+//           (the same launch voids the query-cache margins of the body's cloth)
+//   boxes   expanded triangle boxes (primitive.cu:79-91) and leaf records, three
+//           corners gathered as aligned float4; per CTA the union of its boxes
+//           with the identity box
+//   codes   the Morton frame (identity box U every box: each CTA reduces the CTA
+//           unions itself); the Morton code of each box centroid in the frame
+//           (bvh.cu:20-41,71-79; bbox.h:97-127); codes that differ from the last
+//           build's are listed
+//   sort    the stable order by (code, triangle).  When the last build's sorted
+//           list is at hand and at most CHG_CAP codes changed (a body that moves
+//           rigidly flips a few codes at cell edges), it is merged: the unchanged
+//           entries keep their order, every CTA sorts the changed ones in shared
+//           memory, and each entry's new position follows from binary searches
+//           (phase_merge).  Otherwise four stable LSD radix passes over 8-bit
+//           digits, tiles claimed in order, decoupled look-back.
+//   unique  keep the first triangle of every distinct code (remove_redundant,
+//           Utilities.h:35-55): per-CTA counts, a barrier, then each CTA's offset
+//   build   bottom-up radix-tree build fused with the refit, per chunk of 512
+//           sorted leaves: each leaf thread climbs with handshakes in shared
+//           memory while both children lie in the chunk; the parent of range
+//           [l, r] is the boundary with the longer common prefix (delta(l-1,l)
+//           vs delta(r,r+1), delta = clz(a ^ b) as cudaBRT.cu:9-19), the second
+//           child to arrive merges both boxes into the identity box
+//           (calculateBoudingBox, cudaBRT.cu:166-206) and continues.  Each chunk
+//           then publishes a summary for the nodes that span chunks; the CTA that
+//           finishes the last chunk of a group of 32 sums the group up a level
+//   top     one warp per node that spans chunks: its range ends are the nearest
+//           boundaries with a smaller delta, its box the union of its leaves'
+//           boxes, both read off the chunk summaries
+// Nodes are numbered by their split position; the tree is the same binary radix
+// tree processInternalNode (cudaBRT.cu:120-161) builds, and visg_export_lbvh
+// renumbers it into the reference's layout.  Data one CTA reads after another wrote
+// it in the same launch is loaded through L2 (ld.global.cg), never the read-only
+// path.  Every wait is bounded; a wait that gives up sets ERR_TIMEOUT, the CTA skips
+// the rest of its work (still arriving at each barrier), and the host reports
 // VISG_ERR_TIMEOUT.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "visg_internal.cuh"
 
@@ -45,28 +56,32 @@ namespace visg {
 
 namespace {
 
-constexpr int BUILD_THREADS = 256;
-constexpr int SORT_THREADS = 256;
-constexpr int SORT_ITEMS = 8;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;  // 2048
+constexpr int RB = 512;        // threads per CTA: one chunk of leaves, one leaf per thread
+constexpr int RW = RB / 32;    // warps per CTA
+constexpr int SORT_ITEMS = 4;
+constexpr int SORT_TILE = RB * SORT_ITEMS;  // 2048 keys per radix tile
 constexpr int RADIX = 256;
 constexpr int PASSES = 4;
-static_assert(PASSES % 2 == 0, "the last pass writes keys[1] / vals[1], which k_coherence reads");
+constexpr int UNIQ_ITEMS = 4;
+constexpr int CHG_CAP = 2048;  // changed codes the incremental sort merges
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_PREFIX = 2u << 30;
 constexpr uint32_t ST_VALUE = (1u << 30) - 1u;
 constexpr int SPIN_LIMIT = 1 << 22;
-// rebuild mode word (zero before every build): what k_coherence found
-constexpr uint32_t M_RAN = 1u;       // the check ran (else every pass does its work)
-constexpr uint32_t M_UNSORTED = 2u;  // the last permutation does not sort the new codes
-constexpr uint32_t M_CHANGED = 4u;   // some code changed
-__device__ __forceinline__ bool skip_sort(uint32_t m) { return (m & M_RAN) && !(m & M_UNSORTED); }
-__device__ __forceinline__ bool skip_unique(uint32_t m) { return (m & M_RAN) && !(m & (M_UNSORTED | M_CHANGED)); }
+constexpr uint64_t kGridWaitNs = 1000000000ull;  // a grid barrier gives up after 1 s
+constexpr int BUILD_LEAVES = RB;                 // leaves per chunk
+constexpr int NLEV = 4;
+constexpr int BIG_DELTA = 64;  // above every delta: a boundary that does not exist
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) {
     return *reinterpret_cast<const volatile uint32_t*>(p);
 }
 __device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *reinterpret_cast<volatile uint32_t*>(p) = v; }
+__device__ __forceinline__ uint64_t now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Decoupled look-back: the exclusive prefix of tile `tile` from the status words of
 // the tiles before it (tile t's at st0[t * stride]: 0 = not yet published, ST_AGG |
@@ -106,7 +121,8 @@ __device__ __forceinline__ uint32_t look_back(const uint32_t* st0, size_t stride
     return excl;
 }
 
-// inclusive scan of one value per thread over a 256-thread block
+// inclusive scan of one value per thread over the CTA (s_warp: 32 words); the CTA
+// total is left in s_warp[RW - 1]
 __device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* s_warp) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -117,37 +133,138 @@ __device__ __forceinline__ uint32_t block_scan_incl(uint32_t v, uint32_t* s_warp
     if (lane == 31) s_warp[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0u;
+        uint32_t w = lane < RW ? s_warp[lane] : 0u;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
             if (lane >= o) w += t;
         }
-        if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = w;
+        if (lane < RW) s_warp[lane] = w;
     }
     __syncthreads();
     uint32_t r = v + (warp > 0 ? s_warp[warp - 1] : 0u);
     __syncthreads();
     return r;
 }
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* s_warp) {
+    (void)block_scan_incl(v, s_warp);
+    const uint32_t t = s_warp[RW - 1];
+    __syncthreads();  // every thread has read it before the next scan writes s_warp
+    return t;
+}
 
-// ------------------------------------------------------------------------------------------
-__global__ void k_body_prep(const float* __restrict__ xyz, const float* __restrict__ nrm, int nv, float thickness,
-                            float4* __restrict__ verts, BvhRoot* root, int nt) {
-    int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v == 0) {
-        root->acc[0] = root->acc[1] = root->acc[2] = f2ord(100.0f);   // identity box min (bbox.h:17-22)
-        root->acc[3] = root->acc[4] = root->acc[5] = f2ord(-100.0f);  // identity box max
-        root->n_tris = nt;
+// ---- arguments and shared memory ------------------------------------------------------------
+struct ChunkView {
+    int* cmin;
+    float4* cbox;
+    int2* srec;
+    float4* sbox;
+    int2* prec;
+    float4* pbox;
+    int* rcnt;
+    int2* top;
+    int lev_off[NLEV];
+};
+
+struct RebuildArgs {
+    const float* xyz;
+    const float* nrm;  // null: no thickness push
+    const uint32_t* tris;
+    int nv, nt;
+    float thickness, depth;
+    int coherent;  // the last build's sorted list and codes may be reused
+    int tiles_sort;
+    float4* verts;
+    float4* tri_box;
+    float4* tri_leaf;
+    uint32_t* codes;
+    uint32_t* keys[2];
+    uint32_t* vals[2];
+    uint32_t* ucode;
+    uint32_t* utri;
+    Node* nodes;
+    float4* leaves;
+    int2* range;
+    BvhRoot* root;
+    ChunkView cv;
+    uint32_t* ghist;   // PASSES x RADIX digit counts
+    uint32_t* sstat;   // PASSES x tiles_sort x RADIX look-back status words
+    uint32_t* scount;  // PASSES tile counters
+    float* part;       // 8 per CTA: its box union (min xyz, max xyz)
+    uint32_t* ucnt;    // per CTA: distinct codes in its slice of the sorted list
+    uint32_t* chg;     // [0] changed codes, then {triangle, new code, old code} x CHG_CAP
+    uint32_t* sync;    // [0] barrier arrivals, [1] CTAs finished (both 0 between launches)
+    uint32_t* gdone;   // per summary entry of levels 1..3: its member entries finished
+    int n_entries;     // summary entries of all levels
+    int* err;
+    float4* margin_state;  // cloth records whose query-cache margins the moved body voids
+    int64_t m0, m1;        // (vertices [m0, m1): their margin words are cleared)
+};
+
+struct BuildSmem {
+    uint32_t flag[BUILD_LEAVES];  // bit 0: child A arrived, bit 1: child B
+    // per node and side (A, B): lo (w = link), hi (w = far range end)
+    float4 lo[BUILD_LEAVES][2], hi[BUILD_LEAVES][2];
+    int delta[BUILD_LEAVES + 4];  // delta of boundary j at j - c0 + 1
+    int wmin[RW], wsr[RW], wpr[RW], wtop[RW];  // per warp
+    float4 wlo[RW], whi[RW];
+    // per warp, over the warps before (x*p) / after (x*s) it
+    int xpm[RW], xsm[RW], xos[RW], xop[RW], xot[RW];
+    float4 xplo[RW], xphi[RW], xslo[RW], xshi[RW];
+    int nrec[4];
+};
+struct SortSmem {
+    uint32_t whist[RW][RADIX + 1];
+    uint32_t tstart[RADIX];
+    uint32_t gbase[RADIX];
+    uint32_t keys[SORT_TILE];
+    uint32_t vals[SORT_TILE];
+};
+struct MergeSmem {
+    unsigned long long knew[CHG_CAP];  // changed entries by (new code, triangle)
+    unsigned long long kold[CHG_CAP];  // the same entries by (old code, triangle)
+};
+constexpr size_t smax(size_t a, size_t b) { return a > b ? a : b; }
+constexpr size_t kSmemBytes = smax(sizeof(BuildSmem), smax(sizeof(SortSmem), sizeof(MergeSmem)));
+
+// ---- grid barrier ---------------------------------------------------------------------------
+// Every CTA arrives on sync[0] and waits until it holds `target` (gridDim.x per
+// barrier so far).  A CTA whose earlier wait gave up (ok false) still arrives, so
+// the others are not held, but does not wait.  Returns whether this CTA may go on.
+__device__ bool grid_barrier(uint32_t* ctr, uint32_t& target, bool ok, int* err, int* s_ok) {
+    __syncthreads();
+    target += gridDim.x;
+    if (threadIdx.x == 0) {
+        __threadfence();  // this CTA's writes before its arrival
+        atomicAdd(ctr, 1u);
+        int good = ok ? 1 : 0;
+        if (good && ld_volatile(ctr) < target) {
+            const uint64_t t0 = now_ns();
+            while (ld_volatile(ctr) < target) {
+                if (now_ns() - t0 > kGridWaitNs) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();  // the others' writes before this CTA's reads
+        *s_ok = good;
     }
-    if (v >= nv) return;
-    float x = xyz[3 * v], y = xyz[3 * v + 1], z = xyz[3 * v + 2];
-    if (nrm) {
-        x = __fadd_rn(x, __fmul_rn(thickness, nrm[3 * v]));
-        y = __fadd_rn(y, __fmul_rn(thickness, nrm[3 * v + 1]));
-        z = __fadd_rn(z, __fmul_rn(thickness, nrm[3 * v + 2]));
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// ---- boxes ------------------------------------------------------------------------------------
+__device__ __forceinline__ f3 pushed(const RebuildArgs& A, uint32_t v) {  // vertex_extend
+    float x = __ldg(A.xyz + 3 * v), y = __ldg(A.xyz + 3 * v + 1), z = __ldg(A.xyz + 3 * v + 2);
+    if (A.nrm) {
+        x = __fadd_rn(x, __fmul_rn(A.thickness, __ldg(A.nrm + 3 * v)));
+        y = __fadd_rn(y, __fmul_rn(A.thickness, __ldg(A.nrm + 3 * v + 1)));
+        z = __fadd_rn(z, __fmul_rn(A.thickness, __ldg(A.nrm + 3 * v + 2)));
     }
-    verts[v] = make_float4(x, y, z, 0.0f);
+    return mk3(x, y, z);
 }
 
 __device__ __forceinline__ void box_add(f3& lo, f3& hi, f3 p) {
@@ -155,43 +272,8 @@ __device__ __forceinline__ void box_add(f3& lo, f3& hi, f3 p) {
     hi.x = fmaxf(hi.x, p.x); hi.y = fmaxf(hi.y, p.y); hi.z = fmaxf(hi.z, p.z);
 }
 
-__global__ void __launch_bounds__(BUILD_THREADS)
-k_tri_boxes(const float4* __restrict__ verts, int nv, const uint32_t* __restrict__ tris, int nt, float depth,
-            float4* __restrict__ tri_box, float4* __restrict__ tri_leaf, BvhRoot* root, int* err) {
-    __shared__ float s_red[6][BUILD_THREADS / 32];
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    f3 lo = mk3(100.0f, 100.0f, 100.0f), hi = mk3(-100.0f, -100.0f, -100.0f);
-    if (t < nt) {
-        // vertex indices come from the caller: one out of range is recorded and read
-        // as vertex 0, so no load leaves the vertex array (the build's result is then
-        // reported as failed)
-        uint32_t i0 = tris[3 * t], i1 = tris[3 * t + 1], i2 = tris[3 * t + 2];
-        if (i0 >= (uint32_t)nv || i1 >= (uint32_t)nv || i2 >= (uint32_t)nv) {
-            atomicOr(err, ERR_INDEX);
-            i0 = i0 < (uint32_t)nv ? i0 : 0u;
-            i1 = i1 < (uint32_t)nv ? i1 : 0u;
-            i2 = i2 < (uint32_t)nv ? i2 : 0u;
-        }
-        f3 v0 = xyz(__ldg(&verts[i0]));
-        f3 v1 = xyz(__ldg(&verts[i1]));
-        f3 v2 = xyz(__ldg(&verts[i2]));
-        f3 n = normalize(cross(sub(v1, v0), sub(v2, v0)));  // Primitive::d_get_normal
-        f3 blo = v0, bhi = v0;                                 // BBox(v0).expand(v1).expand(v2)
-        box_add(blo, bhi, v1);
-        box_add(blo, bhi, v2);
-        f3 dn = mul(depth, n);
-        box_add(blo, bhi, sub(v0, dn));
-        box_add(blo, bhi, sub(v1, dn));
-        box_add(blo, bhi, sub(v2, dn));
-        tri_box[2 * t] = make_float4(blo.x, blo.y, blo.z, 0.0f);
-        tri_box[2 * t + 1] = make_float4(bhi.x, bhi.y, bhi.z, 0.0f);
-        tri_leaf[2 * t] = make_float4(v0.x, v0.y, v0.z, n.x);
-        tri_leaf[2 * t + 1] = make_float4(n.y, n.z, __int_as_float(t), 0.0f);
-        lo = blo;
-        hi = bhi;
-    }
-    // frame = identity U every box: block min/max, then one ordered atomic per block
-    float r[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+// min (k < 3) / max (k >= 3) of r[6] over the CTA, into s_red[6] (all threads)
+__device__ __forceinline__ void block_box_reduce(float r[6], float* s_red /* 6 * RW */) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -201,17 +283,87 @@ k_tri_boxes(const float4* __restrict__ verts, int nv, const uint32_t* __restrict
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0)
-        for (int k = 0; k < 6; ++k) s_red[k][warp] = r[k];
+        for (int k = 0; k < 6; ++k) s_red[k * RW + warp] = r[k];
     __syncthreads();
     if (threadIdx.x < 6) {
-        int k = threadIdx.x;
-        float v = s_red[k][0];
-        for (int w = 1; w < BUILD_THREADS / 32; ++w) v = k < 3 ? fminf(v, s_red[k][w]) : fmaxf(v, s_red[k][w]);
-        if (k < 3) atomicMin(&root->acc[k], f2ord(v));
-        else atomicMax(&root->acc[k], f2ord(v));
+        const int k = threadIdx.x;
+        float v = s_red[k * RW];
+        for (int w = 1; w < RW; ++w) v = k < 3 ? fminf(v, s_red[k * RW + w]) : fmaxf(v, s_red[k * RW + w]);
+        s_red[k * RW] = v;
     }
+    __syncthreads();
 }
 
+// the pushed vertices, as float4 (one aligned load per corner in phase_boxes); the
+// query-cache margins of the body's cloth vertices are voided (the body moves)
+__device__ void phase_verts(const RebuildArgs& A) {
+    for (int v = blockIdx.x * RB + threadIdx.x; v < A.nv; v += gridDim.x * RB) {
+        const f3 p = pushed(A, (uint32_t)v);
+        A.verts[v] = make_float4(p.x, p.y, p.z, 0.0f);
+    }
+    if (A.margin_state)
+        for (int64_t i = A.m0 + (int64_t)blockIdx.x * RB + threadIdx.x; i < A.m1; i += (int64_t)gridDim.x * RB)
+            reinterpret_cast<float*>(A.margin_state + 2 * i + 1)[3] = 0.0f;
+}
+
+constexpr int BOX_BATCH = 3;  // triangles a thread loads before it computes any
+
+// each triangle's expanded box (BBox(v0).expand(v1).expand(v2) and the three
+// corners pushed inward by depth * n) and leaf record; the CTA's union of its boxes
+// with the identity box in part[8 * cta]
+__device__ void phase_boxes(const RebuildArgs& A, float* s_red) {
+    const int stride = gridDim.x * RB;
+    f3 lo = mk3(100.0f, 100.0f, 100.0f), hi = mk3(-100.0f, -100.0f, -100.0f);
+    for (int base = blockIdx.x * RB + threadIdx.x; base < A.nt; base += BOX_BATCH * stride) {
+        uint32_t idx[BOX_BATCH][3];
+#pragma unroll
+        for (int q = 0; q < BOX_BATCH; ++q) {
+            const int t = base + q * stride;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) idx[q][c] = t < A.nt ? __ldg(A.tris + 3 * t + c) : 0u;
+        }
+        float4 w[BOX_BATCH][3];
+#pragma unroll
+        for (int q = 0; q < BOX_BATCH; ++q)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                // vertex indices come from the caller: one out of range is recorded and
+                // read as vertex 0, so no load leaves the vertex array (the build's
+                // result is then reported as failed)
+                uint32_t v = idx[q][c];
+                if (v >= (uint32_t)A.nv) {
+                    if (base + q * stride < A.nt) atomicOr(A.err, ERR_INDEX);
+                    v = 0u;
+                }
+                w[q][c] = __ldcg(A.verts + v);
+            }
+#pragma unroll
+        for (int q = 0; q < BOX_BATCH; ++q) {
+            const int t = base + q * stride;
+            if (t >= A.nt) break;
+            const f3 v0 = xyz(w[q][0]), v1 = xyz(w[q][1]), v2 = xyz(w[q][2]);
+            const f3 n = normalize(cross(sub(v1, v0), sub(v2, v0)));  // Primitive::d_get_normal
+            f3 blo = v0, bhi = v0;
+            box_add(blo, bhi, v1);
+            box_add(blo, bhi, v2);
+            const f3 dn = mul(A.depth, n);
+            box_add(blo, bhi, sub(v0, dn));
+            box_add(blo, bhi, sub(v1, dn));
+            box_add(blo, bhi, sub(v2, dn));
+            A.tri_box[2 * t] = make_float4(blo.x, blo.y, blo.z, 0.0f);
+            A.tri_box[2 * t + 1] = make_float4(bhi.x, bhi.y, bhi.z, 0.0f);
+            A.tri_leaf[2 * t] = make_float4(v0.x, v0.y, v0.z, n.x);
+            A.tri_leaf[2 * t + 1] = make_float4(n.y, n.z, __int_as_float(t), 0.0f);
+            box_add(lo, hi, blo);
+            box_add(lo, hi, bhi);
+        }
+    }
+    float r[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+    block_box_reduce(r, s_red);
+    if (threadIdx.x < 6) A.part[8 * blockIdx.x + threadIdx.x] = s_red[threadIdx.x * RW];
+}
+
+// ---- codes ------------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {  // bvh.cu:20-27
     v = (v * 0x00010001u) & 0xFF0000FFu;
     v = (v * 0x00000101u) & 0x0F00F00Fu;
@@ -220,116 +372,232 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {  // bvh.cu:20-27
     return v;
 }
 
-__global__ void __launch_bounds__(BUILD_THREADS)
-k_morton(const float4* __restrict__ tri_box, int nt, BvhRoot* root, uint32_t* __restrict__ codes,
-         uint32_t* __restrict__ ghist /* PASSES*RADIX */) {
-    __shared__ uint32_t s_hist[PASSES][RADIX];
-    __shared__ float s_frame[6];
-    for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) (&s_hist[0][0])[k] = 0;
-    if (threadIdx.x < 6) s_frame[threadIdx.x] = ord2f(root->acc[threadIdx.x]);
-    __syncthreads();
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        root->frame_lo = make_float4(s_frame[0], s_frame[1], s_frame[2], 0.0f);
-        root->frame_hi = make_float4(s_frame[3], s_frame[4], s_frame[5], 0.0f);
-    }
-    uint32_t code = 0u;
-    if (t < nt) {
-        float4 lo = tri_box[2 * t], hi = tri_box[2 * t + 1];
-        f3 c = divs(add(xyz(lo), xyz(hi)), 2.0f);  // BBox::centroid
-        f3 fmn = mk3(s_frame[0], s_frame[1], s_frame[2]);
-        f3 ext = sub(mk3(s_frame[3], s_frame[4], s_frame[5]), fmn);
-        f3 q = mk3(0.0f, 0.0f, 0.0f);
-        if (length(ext) != 0.0f) q = divv(sub(c, fmn), ext);  // BBox::getUnitcubePosOf
-        float x = fminf(fmaxf(__fmul_rn(q.x, 1024.0f), 0.0f), 1023.0f);
-        float y = fminf(fmaxf(__fmul_rn(q.y, 1024.0f), 0.0f), 1023.0f);
-        float z = fminf(fmaxf(__fmul_rn(q.z, 1024.0f), 0.0f), 1023.0f);
-        code = expand_bits((uint32_t)x) * 4u + expand_bits((uint32_t)y) * 2u + expand_bits((uint32_t)z);
-        codes[t] = code;
-    }
-    // digit counts of the four radix passes; the two high digits are nearly constant
-    // across a block's neighbouring triangles, so their lanes add once per equal digit
-    const int lane = threadIdx.x & 31;
-    const bool ok = t < nt;
+// the frame from the CTA unions; each triangle's code; with `listing`, the triangles
+// whose code changed go to the change list (at most CHG_CAP are stored)
+__device__ void phase_codes(const RebuildArgs& A, bool listing, float* s_red, float* s_frame) {
+    float r[6] = {100.0f, 100.0f, 100.0f, -100.0f, -100.0f, -100.0f};
+    for (int c = threadIdx.x; c < (int)gridDim.x; c += RB) {
 #pragma unroll
-    for (int p = 0; p < PASSES; ++p) {
-        const uint32_t dig = (code >> (8 * p)) & 255u;
-        if (p < 2) {
-            if (ok) atomicAdd(&s_hist[p][dig], 1u);
-        } else {
-            const uint32_t peers = __match_any_sync(0xffffffffu, ok ? dig : RADIX);
-            if (ok && lane == __ffs(peers) - 1) atomicAdd(&s_hist[p][dig], (uint32_t)__popc(peers));
-        }
+        for (int k = 0; k < 3; ++k) r[k] = fminf(r[k], __ldcg(A.part + 8 * c + k));
+#pragma unroll
+        for (int k = 3; k < 6; ++k) r[k] = fmaxf(r[k], __ldcg(A.part + 8 * c + k));
     }
+    block_box_reduce(r, s_red);
+    if (threadIdx.x < 6) s_frame[threadIdx.x] = s_red[threadIdx.x * RW];
     __syncthreads();
-    for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) {
-        uint32_t v = (&s_hist[0][0])[k];
-        if (v) atomicAdd(&ghist[k], v);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        A.root->frame_lo = make_float4(s_frame[0], s_frame[1], s_frame[2], 0.0f);
+        A.root->frame_hi = make_float4(s_frame[3], s_frame[4], s_frame[5], 0.0f);
     }
-}
-
-// Temporal coherence of a rebuild.  keys1/vals1 hold the last build's sorted codes
-// and permutation (when root->perm_valid).  The stable sort of the new codes by
-// (code, triangle) is unique, so if the last permutation orders them (non-decreasing
-// codes, equal codes by increasing triangle), it is that sort: keys1 takes the new
-// codes in that order and the radix passes have nothing to do.  If no code changed,
-// the de-duplicated leaves are the last build's too.
-__global__ void __launch_bounds__(BUILD_THREADS)
-k_coherence(const uint32_t* __restrict__ codes, uint32_t* keys1, const uint32_t* __restrict__ vals1, int nt,
-            const BvhRoot* __restrict__ root, uint32_t* mode) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t bad = 0;
-    if (!root->perm_valid) {
-        bad = M_UNSORTED | M_CHANGED;
-    } else if (i < nt) {
-        const uint32_t p = vals1[i];
-        if (p >= (uint32_t)nt) {
-            bad = M_UNSORTED | M_CHANGED;
-        } else {
-            const uint32_t c = codes[p];
-            if (c != keys1[i]) bad |= M_CHANGED;
-            if (i > 0) {
-                const uint32_t q = vals1[i - 1];
-                const uint32_t cq = q < (uint32_t)nt ? codes[q] : 0xffffffffu;
-                if (q >= (uint32_t)nt || cq > c || (cq == c && q > p)) bad |= M_UNSORTED;
+    const f3 fmn = mk3(s_frame[0], s_frame[1], s_frame[2]);
+    const f3 ext = sub(mk3(s_frame[3], s_frame[4], s_frame[5]), fmn);
+    const bool flat = length(ext) == 0.0f;
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * RB;
+    for (int base = blockIdx.x * RB; base < A.nt; base += 2 * stride) {  // warp-uniform bounds
+        // both triangles' loads first
+        float4 blo[2], bhi[2];
+        uint32_t old[2] = {0u, 0u};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int t = base + q * stride + threadIdx.x;
+            if (t < A.nt) {
+                blo[q] = __ldcg(A.tri_box + 2 * t);
+                bhi[q] = __ldcg(A.tri_box + 2 * t + 1);
+                if (listing) old[q] = A.codes[t];
             }
-            keys1[i] = c;  // only this thread reads or writes entry i
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int t = base + q * stride + threadIdx.x;
+            bool changed = false;
+            uint32_t code = 0u;
+            if (t < A.nt) {
+                const f3 c = divs(add(xyz(blo[q]), xyz(bhi[q])), 2.0f);  // BBox::centroid
+                f3 u = mk3(0.0f, 0.0f, 0.0f);
+                if (!flat) u = divv(sub(c, fmn), ext);  // BBox::getUnitcubePosOf
+                const float x = fminf(fmaxf(__fmul_rn(u.x, 1024.0f), 0.0f), 1023.0f);
+                const float y = fminf(fmaxf(__fmul_rn(u.y, 1024.0f), 0.0f), 1023.0f);
+                const float z = fminf(fmaxf(__fmul_rn(u.z, 1024.0f), 0.0f), 1023.0f);
+                code = expand_bits((uint32_t)x) * 4u + expand_bits((uint32_t)y) * 2u + expand_bits((uint32_t)z);
+                A.codes[t] = code;
+                changed = listing && old[q] != code;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, changed);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                uint32_t b0 = 0;
+                if (lane == leader) b0 = atomicAdd(A.chg, (uint32_t)__popc(m));
+                b0 = __shfl_sync(0xffffffffu, b0, leader);
+                const uint32_t k = b0 + (uint32_t)__popc(m & ((1u << lane) - 1u));
+                if (changed && k < (uint32_t)CHG_CAP) {
+                    A.chg[1 + 3 * k] = (uint32_t)t;
+                    A.chg[2 + 3 * k] = code;
+                    A.chg[3 + 3 * k] = old[q];
+                }
+            }
         }
     }
-    bad = __reduce_or_sync(0xffffffffu, bad);
-    if ((threadIdx.x & 31) == 0 && bad) atomicOr(mode, bad);
-    if (i == 0) atomicOr(mode, M_RAN);
 }
 
-// One stable LSD pass over 8-bit digit (key >> shift) & 255.  Tiles are claimed in
-// launch order through an atomic counter, so every tile a block waits on belongs to a
-// block that is already running: the look-back always terminates.
-__global__ void __launch_bounds__(SORT_THREADS)
-k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-            uint32_t* __restrict__ vout, int n, int shift, const uint32_t* __restrict__ ghist,
-            uint32_t* status, uint32_t* counter, const uint32_t* __restrict__ mode, int* err) {
-    if (skip_sort(*mode)) return;  // the last build's order stands
-    __shared__ uint32_t s_whist[SORT_THREADS / 32][RADIX + 1];
-    __shared__ uint32_t s_tstart[RADIX];
-    __shared__ uint32_t s_gbase[RADIX];
-    __shared__ uint32_t s_keys[SORT_TILE];
-    __shared__ uint32_t s_vals[SORT_TILE];
-    __shared__ uint32_t s_warp[32];
-    __shared__ int s_tile;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_tile = (int)atomicAdd(counter, 1u);
-    for (int k = tid; k < (SORT_THREADS / 32) * (RADIX + 1); k += SORT_THREADS) (&s_whist[0][0])[k] = 0;
+// ---- sort: incremental merge --------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long key64(uint32_t code, uint32_t tri) {
+    return ((unsigned long long)code << 32) | tri;
+}
+// entries of a[0, n) below x (a ascending)
+__device__ __forceinline__ int lower_bound64(const unsigned long long* a, int n, unsigned long long x) {
+    int lo = 0, len = n;
+    while (len > 0) {
+        const int h = len >> 1;
+        if (a[lo + h] < x) {
+            lo += h + 1;
+            len -= h + 1;
+        } else {
+            len = h;
+        }
+    }
+    return lo;
+}
+
+// Merge of the nc changed entries into the last build's sorted list ko/vo (all nt
+// triangles by (code, triangle), old codes): every CTA sorts the changed entries by
+// new key (knew) and by old key (kold), then walks its slice of the old list.  For
+// old slot s with key k_s, q(s) = #kold < k_s and r(s) = #knew < k_s.  An unchanged
+// entry keeps its code, so its key is k_s and its new position is s - q(s) (the
+// unchanged entries before it) + r(s) (the changed entries that now sort before
+// it).  Changed entry j with r(s) <= j < r(s + 1) lies strictly between k_s and
+// k_(s+1): s + 1 - q(s + 1) unchanged entries sort before it, j changed ones, so its
+// position is j + s + 1 - q(s + 1).  Changed entries below the first old key go to
+// positions j (CTA 0).  Positions are a permutation of [0, nt); each is checked.
+__device__ void phase_merge(const RebuildArgs& A, int nc, const uint32_t* ko, const uint32_t* vo, uint32_t* kn,
+                            uint32_t* vn, MergeSmem& S) {
+    int P = 1;
+    while (P < nc) P <<= 1;
+    for (int k = threadIdx.x; k < P; k += RB) {
+        if (k < nc) {
+            const uint32_t t = __ldcg(A.chg + 1 + 3 * k);
+            S.knew[k] = key64(__ldcg(A.chg + 2 + 3 * k), t);
+            S.kold[k] = key64(__ldcg(A.chg + 3 + 3 * k), t);
+        } else {
+            S.knew[k] = S.kold[k] = ~0ull;
+        }
+    }
     __syncthreads();
-    const int tile = s_tile;
+    for (int k = 2; k <= P; k <<= 1)  // bitonic sort of both arrays, ascending
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += RB) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const unsigned long long a = S.knew[i], b = S.knew[l];
+                    if ((a > b) == up) {
+                        S.knew[i] = b;
+                        S.knew[l] = a;
+                    }
+                    const unsigned long long c = S.kold[i], d = S.kold[l];
+                    if ((c > d) == up) {
+                        S.kold[i] = d;
+                        S.kold[l] = c;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    const int nt = A.nt;
+    const int per = (nt + gridDim.x - 1) / gridDim.x;
+    const int a = blockIdx.x * per, b = min(nt, a + per);
+    constexpr int MB = 3;  // slots a thread loads before it searches
+    for (int s0 = a + threadIdx.x; s0 < b; s0 += MB * RB) {
+        unsigned long long ks[MB], k1[MB];
+#pragma unroll
+        for (int u = 0; u < MB; ++u) {
+            const int s = s0 + u * RB;
+            ks[u] = s < b ? key64(ko[s], vo[s]) : ~0ull;
+            k1[u] = s < b && s + 1 < nt ? key64(ko[s + 1], vo[s + 1]) : ~0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < MB; ++u) {
+            const int s = s0 + u * RB;
+            if (s >= b) break;
+            const int q = lower_bound64(S.kold, nc, ks[u]);
+            const int r = lower_bound64(S.knew, nc, ks[u]);
+            if (!(q < nc && S.kold[q] == ks[u])) {  // unchanged
+                const int pos = s - q + r;
+                if ((unsigned)pos < (unsigned)nt) {
+                    kn[pos] = (uint32_t)(ks[u] >> 32);
+                    vn[pos] = (uint32_t)ks[u];
+                }
+            }
+            int r1 = nc, q1 = nc;
+            if (s + 1 < nt) {
+                r1 = lower_bound64(S.knew, nc, k1[u]);
+                q1 = lower_bound64(S.kold, nc, k1[u]);
+            }
+            for (int j = r; j < r1; ++j) {
+                const int pos = j + s + 1 - q1;
+                if ((unsigned)pos < (unsigned)nt) {
+                    kn[pos] = (uint32_t)(S.knew[j] >> 32);
+                    vn[pos] = (uint32_t)S.knew[j];
+                }
+            }
+        }
+    }
+    if (blockIdx.x == 0 && nt > 0) {
+        const int r0 = lower_bound64(S.knew, nc, key64(ko[0], vo[0]));
+        for (int j = threadIdx.x; j < r0; j += RB) {
+            kn[j] = (uint32_t)(S.knew[j] >> 32);
+            vn[j] = (uint32_t)S.knew[j];
+        }
+    }
+}
+
+// ---- sort: radix passes ------------------------------------------------------------------------
+// digit counts of all four passes (grid-stride over the codes, per CTA in shared memory)
+__device__ void phase_hist(const RebuildArgs& A, uint32_t* s_hist /* PASSES * RADIX */) {
+    for (int k = threadIdx.x; k < PASSES * RADIX; k += RB) s_hist[k] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * RB; base < A.nt; base += gridDim.x * RB) {
+        const int t = base + threadIdx.x;
+        const bool ok = t < A.nt;
+        const uint32_t code = ok ? __ldcg(A.codes + t) : 0u;
+        // the two high digits are nearly constant across neighbouring triangles, so
+        // their lanes add once per equal digit
+#pragma unroll
+        for (int p = 0; p < PASSES; ++p) {
+            const uint32_t dig = (code >> (8 * p)) & 255u;
+            if (p < 2) {
+                if (ok) atomicAdd(&s_hist[p * RADIX + dig], 1u);
+            } else {
+                const uint32_t peers = __match_any_sync(0xffffffffu, ok ? dig : RADIX);
+                if (ok && lane == __ffs(peers) - 1) atomicAdd(&s_hist[p * RADIX + dig], (uint32_t)__popc(peers));
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < PASSES * RADIX; k += RB) {
+        const uint32_t v = s_hist[k];
+        if (v) atomicAdd(&A.ghist[k], v);
+    }
+}
+
+// One tile of a stable LSD pass over 8-bit digit (key >> shift) & 255.  Tiles are
+// claimed in order through a counter, so every tile a CTA waits on belongs to a CTA
+// that is already at work on it: the look-back always terminates.
+__device__ void sort_tile(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int n, int shift,
+                          const uint32_t* ghist, uint32_t* status, int tile, SortSmem& S, uint32_t* s_scan, int* err) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int k = tid; k < RW * (RADIX + 1); k += RB) (&S.whist[0][0])[k] = 0;
+    __syncthreads();
     const int base = tile * SORT_TILE + warp * (32 * SORT_ITEMS);
     uint32_t key[SORT_ITEMS], val[SORT_ITEMS], rank[SORT_ITEMS];
     int dig[SORT_ITEMS];
 #pragma unroll
     for (int j = 0; j < SORT_ITEMS; ++j) {
-        int idx = base + j * 32 + lane;  // warp-striped: j-major order is input order
+        const int idx = base + j * 32 + lane;  // warp-striped: j-major order is input order
         if (idx < n) {
-            key[j] = kin[idx];
-            val[j] = vin ? vin[idx] : (uint32_t)idx;
+            key[j] = __ldcg(kin + idx);
+            val[j] = vin ? __ldcg(vin + idx) : (uint32_t)idx;
             dig[j] = (int)((key[j] >> shift) & 255u);
         } else {
             key[j] = 0u;
@@ -340,126 +608,144 @@ k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, 
     // stable rank of every key among equal digits of this warp, in input order
 #pragma unroll
     for (int j = 0; j < SORT_ITEMS; ++j) {
-        uint32_t peers = __match_any_sync(0xffffffffu, dig[j]);
-        int leader = __ffs(peers) - 1;
+        const uint32_t peers = __match_any_sync(0xffffffffu, dig[j]);
+        const int leader = __ffs(peers) - 1;
         uint32_t before = 0;
         if (lane == leader) {
-            before = s_whist[warp][dig[j]];
-            s_whist[warp][dig[j]] = before + __popc(peers);
+            before = S.whist[warp][dig[j]];
+            S.whist[warp][dig[j]] = before + __popc(peers);
         }
         before = __shfl_sync(0xffffffffu, before, leader);
         rank[j] = before + __popc(peers & ((1u << lane) - 1u));
         __syncwarp();
     }
     __syncthreads();
-    // thread d owns digit d: warp-exclusive prefixes and the tile count
+    // thread d < RADIX owns digit d: warp-exclusive prefixes and the tile count
     const int d = tid;
-    uint32_t run = 0;
+    uint32_t tcount = 0;
+    if (d < RADIX) {
+        uint32_t run = 0;
 #pragma unroll
-    for (int w = 0; w < SORT_THREADS / 32; ++w) {
-        uint32_t c = s_whist[w][d];
-        s_whist[w][d] = run;
-        run += c;
+        for (int w = 0; w < RW; ++w) {
+            const uint32_t c = S.whist[w][d];
+            S.whist[w][d] = run;
+            run += c;
+        }
+        tcount = run;
     }
-    const uint32_t tcount = run;
-    const uint32_t tincl = block_scan_incl(tcount, s_warp);
-    s_tstart[d] = tincl - tcount;
-    const uint32_t gh = ghist[d];
-    const uint32_t gincl = block_scan_incl(gh, s_warp);
-    const uint32_t goff = gincl - gh;
+    const uint32_t tincl = block_scan_incl(tcount, s_scan);
+    if (d < RADIX) S.tstart[d] = tincl - tcount;
+    const uint32_t gh = d < RADIX ? __ldcg(ghist + d) : 0u;
+    const uint32_t goff = block_scan_incl(gh, s_scan) - gh;
     // publish the tile's count of digit d, then look back for the exclusive prefix
-    uint32_t excl = 0;
-    uint32_t* st = status + (size_t)tile * RADIX + d;
-    if (tile == 0) {
-        st_volatile(st, ST_PREFIX | tcount);
-    } else {
-        st_volatile(st, ST_AGG | tcount);
-        excl = look_back(status + d, RADIX, tile, err);
-        st_volatile(st, ST_PREFIX | ((excl + tcount) & ST_VALUE));
+    if (d < RADIX) {
+        uint32_t excl = 0;
+        uint32_t* st = status + (size_t)tile * RADIX + d;
+        if (tile == 0) {
+            st_volatile(st, ST_PREFIX | tcount);
+        } else {
+            st_volatile(st, ST_AGG | tcount);
+            excl = look_back(status + d, RADIX, tile, err);
+            st_volatile(st, ST_PREFIX | ((excl + tcount) & ST_VALUE));
+        }
+        S.gbase[d] = goff + excl;
     }
-    s_gbase[d] = goff + excl;
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < SORT_ITEMS; ++j) {
         if (dig[j] < RADIX) {
-            uint32_t pos = s_tstart[dig[j]] + s_whist[warp][dig[j]] + rank[j];
-            s_keys[pos] = key[j];
-            s_vals[pos] = val[j];
+            const uint32_t pos = S.tstart[dig[j]] + S.whist[warp][dig[j]] + rank[j];
+            S.keys[pos] = key[j];
+            S.vals[pos] = val[j];
         }
     }
     __syncthreads();
     const int tile_n = min(SORT_TILE, n - tile * SORT_TILE);
-    for (int p = tid; p < tile_n; p += SORT_THREADS) {
-        uint32_t k = s_keys[p];
-        uint32_t dd = (k >> shift) & 255u;
-        uint32_t o = s_gbase[dd] + (uint32_t)p - s_tstart[dd];
+    for (int p = tid; p < tile_n; p += RB) {
+        const uint32_t k = S.keys[p];
+        const uint32_t dd = (k >> shift) & 255u;
+        const uint32_t o = S.gbase[dd] + (uint32_t)p - S.tstart[dd];
         if (o < (uint32_t)n) {  // always true unless a look-back gave up
             kout[o] = k;
-            vout[o] = s_vals[p];
+            vout[o] = S.vals[p];
         }
+    }
+    __syncthreads();
+}
+
+__device__ void phase_sort_pass(const RebuildArgs& A, int p, SortSmem& S, uint32_t* s_scan, int* s_claim) {
+    const uint32_t* kin = p == 0 ? A.codes : A.keys[(p - 1) & 1];
+    const uint32_t* vin = p == 0 ? nullptr : A.vals[(p - 1) & 1];
+    for (;;) {
+        if (threadIdx.x == 0) *s_claim = (int)atomicAdd(A.scount + p, 1u);
+        __syncthreads();
+        const int tile = *s_claim;
+        __syncthreads();
+        if (tile >= A.tiles_sort) break;
+        sort_tile(kin, vin, A.keys[p & 1], A.vals[p & 1], A.nt, 8 * p, A.ghist + p * RADIX,
+                  A.sstat + (size_t)p * A.tiles_sort * RADIX, tile, S, s_scan, A.err);
     }
 }
 
-// keep the first (lowest triangle index) of every run of equal codes
-__global__ void __launch_bounds__(SORT_THREADS)
-k_unique(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int n, uint32_t* __restrict__ ucode,
-         uint32_t* __restrict__ utri, uint32_t* status, uint32_t* counter, int n_tiles, BvhRoot* root,
-         const uint32_t* __restrict__ mode, int* err) {
-    if (skip_unique(*mode)) return;  // same codes: the last build's leaves stand
-    __shared__ uint32_t s_warp[32];
-    __shared__ uint32_t s_excl;
-    __shared__ int s_tile;
-    const int tid = threadIdx.x;
-    if (tid == 0) s_tile = (int)atomicAdd(counter, 1u);
-    __syncthreads();
-    const int tile = s_tile;
-    const int base = tile * SORT_TILE + tid * SORT_ITEMS;
-    uint32_t fl = 0;
-    uint32_t k[SORT_ITEMS];
-    uint32_t prev = base > 0 && base - 1 < n ? keys[base - 1] : 0u;
-#pragma unroll
-    for (int j = 0; j < SORT_ITEMS; ++j) {
-        int i = base + j;
-        k[j] = i < n ? keys[i] : 0u;
-        bool first = i < n && (i == 0 || k[j] != prev);
-        fl |= (first ? 1u : 0u) << j;
-        prev = k[j];
+// ---- unique ------------------------------------------------------------------------------------
+// CTA c takes positions [c * per, (c + 1) * per) of the sorted list; position p is a
+// leaf when p == 0 or its code differs from p - 1's
+__device__ __forceinline__ bool first_of_code(const uint32_t* K, int p) {
+    return p == 0 || __ldcg(K + p) != __ldcg(K + p - 1);
+}
+
+__device__ void phase_unique_count(const RebuildArgs& A, const uint32_t* K, uint32_t* s_scan) {
+    const int per = (A.nt + gridDim.x - 1) / gridDim.x;
+    const int a = blockIdx.x * per, b = min(A.nt, a + per);
+    uint32_t c = 0;
+    for (int p = a + threadIdx.x; p < b; p += RB) c += first_of_code(K, p) ? 1u : 0u;
+    const uint32_t tot = block_sum(c, s_scan);
+    if (threadIdx.x == 0) A.ucnt[blockIdx.x] = tot;
+}
+
+// the leaves of this CTA's slice at its offset (the counts of the CTAs before it);
+// returns the number of leaves in all
+__device__ int phase_unique_write(const RebuildArgs& A, const uint32_t* K, const uint32_t* V, uint32_t* s_scan) {
+    uint32_t before = 0, all = 0;
+    for (int c = threadIdx.x; c < (int)gridDim.x; c += RB) {
+        const uint32_t v = __ldcg(A.ucnt + c);
+        all += v;
+        if (c < (int)blockIdx.x) before += v;
     }
-    const uint32_t cnt = __popc(fl);
-    const uint32_t incl = block_scan_incl(cnt, s_warp);
-    if (tid == SORT_THREADS - 1) {
-        uint32_t tsum = incl;
-        uint32_t excl = 0;
-        uint32_t* st = status + tile;
-        if (tile == 0) {
-            st_volatile(st, ST_PREFIX | tsum);
-        } else {
-            st_volatile(st, ST_AGG | tsum);
-            excl = look_back(status, 1, tile, err);
-            st_volatile(st, ST_PREFIX | ((excl + tsum) & ST_VALUE));
-        }
-        s_excl = excl;
-        if (tile == n_tiles - 1) {
-            root->n_leaves = (int)min(excl + tsum, (uint32_t)n);
-            root->perm_valid = 1;  // k_build withdraws it if a wait of this LBVH build gave up
-        }
-    }
-    __syncthreads();
-    uint32_t o = s_excl + incl - cnt;
+    before = block_sum(before, s_scan);
+    all = block_sum(all, s_scan);
+    const int per = (A.nt + gridDim.x - 1) / gridDim.x;
+    const int a = blockIdx.x * per, b = min(A.nt, a + per);
+    uint32_t off = before;
+    for (int base = a; base < b; base += RB * UNIQ_ITEMS) {
+        const int p0 = base + threadIdx.x * UNIQ_ITEMS;
+        uint32_t fl = 0;
 #pragma unroll
-    for (int j = 0; j < SORT_ITEMS; ++j) {
-        if (fl & (1u << j)) {
-            if (o < (uint32_t)n) {  // always true unless a look-back gave up
-                ucode[o] = k[j];
-                utri[o] = vals[base + j];
+        for (int j = 0; j < UNIQ_ITEMS; ++j)
+            if (p0 + j < b && first_of_code(K, p0 + j)) fl |= 1u << j;
+        const uint32_t cnt = __popc(fl);
+        const uint32_t incl = block_scan_incl(cnt, s_scan);
+        const uint32_t tile_total = s_scan[RW - 1];
+        uint32_t o = off + incl - cnt;
+#pragma unroll
+        for (int j = 0; j < UNIQ_ITEMS; ++j)
+            if (fl & (1u << j)) {
+                if (o < (uint32_t)A.nt) {
+                    A.ucode[o] = __ldcg(K + p0 + j);
+                    A.utri[o] = __ldcg(V + p0 + j);
+                }
+                ++o;
             }
-            ++o;
-        }
+        off += tile_total;
+        __syncthreads();  // s_scan is read above before the next scan overwrites it
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) A.root->n_leaves = (int)min(all, (uint32_t)A.nt);
+    return (int)min(all, (uint32_t)A.nt);
 }
 
+// ---- build ---------------------------------------------------------------------------------------
 __device__ __forceinline__ int delta_at(const uint32_t* c, int i, int j, int n) {
-    return (j < 0 || j >= n) ? -1 : __clz((int)(c[i] ^ c[j]));
+    return (j < 0 || j >= n) ? -1 : __clz((int)(__ldcg(c + i) ^ __ldcg(c + j)));
 }
 
 // identity box (min +100, max -100) expanded by child A then child B
@@ -510,24 +796,6 @@ __device__ __forceinline__ void warp_box_reduce(float4& lo, float4& hi) {
     }
 }
 
-constexpr int BUILD_LEAVES = 512;  // leaves per chunk (one CTA, one leaf per thread)
-
-// Device view of the chunk summaries (see BvhBuffers).
-struct ChunkView {
-    int* cmin;
-    float4* cbox;
-    int2* srec;
-    float4* sbox;
-    int2* prec;
-    float4* pbox;
-    int* rcnt;
-    int2* top;
-    uint32_t* done;
-    int lev_off[4];
-};
-constexpr int NLEV = 4;
-constexpr int BIG_DELTA = 64;  // above every delta: a boundary that does not exist
-
 // entries of each level for n leaves
 __device__ __forceinline__ void level_counts(int n, int cnt[NLEV]) {
     cnt[0] = (n + BUILD_LEAVES - 1) / BUILD_LEAVES;
@@ -535,84 +803,66 @@ __device__ __forceinline__ void level_counts(int n, int cnt[NLEV]) {
     for (int v = 1; v < NLEV; ++v) cnt[v] = (cnt[v - 1] + 31) / 32;
 }
 
-// Bottom-up build of the chunk-local nodes, and the chunk summaries.  Each CTA owns
-// the BUILD_LEAVES sorted leaves [c0, c1) and stages delta of the boundaries
-// c0 - 1 .. c1 - 1.  Phase 1 climbs through the nodes split inside the chunk
-// (c0 <= g <= c1 - 2) in shared memory only: each child leaves its box, link and far
-// range end in its side of the node's slot; the first to arrive stops, the second
-// merges (A then B) and climbs on.  After the barrier the nodes both of whose
-// children arrived are written out; a climb that stopped at a node whose other child
-// lies in another chunk, or at a node split outside the chunk, writes its side into
-// that node.  The remaining nodes span chunks; k_build_top finishes them from the
-// chunk summaries written here:
+// Bottom-up build of the chunk-local nodes, and the chunk summaries.  The CTA owns
+// the BUILD_LEAVES sorted leaves [c0, c1) of `chunk` and stages delta of the
+// boundaries c0 - 1 .. c1 - 1.  The climb goes through the nodes split inside the
+// chunk (c0 <= g <= c1 - 2) in shared memory only: each child leaves its box, link
+// and far range end in its side of the node's slot; the first to arrive stops, the
+// second merges (A then B) and climbs on.  After the barrier the nodes both of
+// whose children arrived are written out; a climb that stopped at a node whose
+// other child lies in another chunk, or at a node split outside the chunk, writes
+// its side into that node.  The remaining nodes span chunks; phase_top finishes them
+// from the chunk summaries written here:
 //   * the boundaries that can end such a node's range inside this chunk: the strict
 //     suffix minima of delta (the nearest smaller delta to the left of a node
 //     further right) and the strict prefix minima (to the right of a node further
 //     left), at most 30 each, with the union of the chunk's leaf boxes beyond /
 //     up to each of them;
-//   * the chunk's min delta and leaf box union (and, from the last CTA to finish,
-//     the same per 32, 1024 and 32768 chunks);
+//   * the chunk's min delta and leaf box union;
 //   * the nodes of the chunk that span chunks (no smaller delta on one side inside
 //     the chunk, and the boundary to the next chunk).
-__global__ void __launch_bounds__(BUILD_LEAVES)
-k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, const float4* __restrict__ tri_box,
-        const float4* __restrict__ tri_leaf, Node* nodes, float4* __restrict__ leaves, int2* range, BvhRoot* root,
-        ChunkView cv, int* err) {
-    __shared__ uint32_t s_flag[BUILD_LEAVES];  // bit 0: child A arrived, bit 1: child B
-    // per node and side (A, B): lo (w = link), hi (w = far range end)
-    __shared__ float4 s_lo[BUILD_LEAVES][2], s_hi[BUILD_LEAVES][2];
-    __shared__ int s_delta[BUILD_LEAVES + 1];  // delta of boundary j at j - c0 + 1
-    constexpr int W = BUILD_LEAVES / 32;
-    __shared__ int s_wmin[W], s_wsr[W], s_wpr[W], s_wtop[W];  // per warp
-    __shared__ float4 s_wlo[W], s_whi[W];
-    // per warp, over the warps before (x*p) / after (x*s) it
-    __shared__ int s_xpm[W], s_xsm[W], s_xos[W], s_xop[W], s_xot[W];
-    __shared__ float4 s_xplo[W], s_xphi[W], s_xslo[W], s_xshi[W];
-    __shared__ int s_nrec[3];
-    __shared__ int s_last;
+__device__ void build_chunk(const RebuildArgs& A, int chunk, int n, BuildSmem& S) {
+    const ChunkView& cv = A.cv;
     const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nt = root->n_tris;
-    const int n = min(root->n_leaves, nt);
-    const int c0 = blockIdx.x * BUILD_LEAVES;
+    const int nt = A.nt;
+    const int c0 = chunk * BUILD_LEAVES;
     const int c1 = min(c0 + BUILD_LEAVES, n);
-    const int chunk = (int)blockIdx.x;
-    if (blockIdx.x == 0 && tid == 0 && (*err & ERR_TIMEOUT)) root->perm_valid = 0;
-    s_flag[tid] = 0u;
+    S.flag[tid] = 0u;
     const int i = c0 + tid;
     int l = i, r = i, link = ~i;  // the current subtree: leaf range, link
     float4 lo = ident_lo(), hi = ident_hi();
     bool live = i < n;  // still climbing
-    int pend = -1;      // node where phase 1 stopped as the first local arrival
-    int out = -1;       // node split outside the chunk where phase 1 stopped
+    int pend = -1;      // node where the climb stopped as the first local arrival
+    int out = -1;       // node split outside the chunk where the climb stopped
     int dl = -1, dr = -1;
     bool is_a = false;
-    uint32_t t = 0;  // the leaf's triangle (its box loads overlap the code loads below)
+    uint32_t t = 0;  // the leaf's triangle
     if (live) {
-        t = min(utri[i], (uint32_t)(nt - 1));
-        lo = tri_box[2 * t];
-        hi = tri_box[2 * t + 1];
+        t = min(__ldcg(A.utri + i), (uint32_t)(nt - 1));
+        lo = __ldcg(A.tri_box + 2 * t);
+        hi = __ldcg(A.tri_box + 2 * t + 1);
     }
     {
         const int j = c0 + tid;
-        s_delta[tid + 1] = delta_at(ucode, j, j + 1, n);  // -1 beyond the last leaf
-        if (tid == 0) s_delta[0] = c0 < n ? delta_at(ucode, c0, c0 - 1, n) : -1;
+        S.delta[tid + 1] = delta_at(A.ucode, j, j + 1, n);  // -1 beyond the last leaf
+        if (tid == 0) S.delta[0] = c0 < n ? delta_at(A.ucode, c0, c0 - 1, n) : -1;
     }
     __syncthreads();
     if (live && n == 1) {
-        root->root = -1;
-        root->top_lo = lo;
-        root->top_hi = hi;
+        A.root->root = -1;
+        A.root->top_lo = lo;
+        A.root->top_hi = hi;
         live = false;
     }
     const float4 leaf_lo = lo, leaf_hi = hi;  // identity box for threads past the last leaf
     int level = 0;
     while (live) {
         if (++level > 64) {  // a climb is at most 31 levels over distinct 30-bit codes
-            atomicOr(err, ERR_TIMEOUT);
+            atomicOr(A.err, ERR_TIMEOUT);
             break;
         }
-        dl = s_delta[l - c0];      // boundary l - 1
-        dr = s_delta[r - c0 + 1];  // boundary r
+        dl = S.delta[l - c0];      // boundary l - 1
+        dr = S.delta[r - c0 + 1];  // boundary r
         is_a = dr > dl;            // the parent extends to the right: this node is child A
         const int g = is_a ? r : l - 1;
         if (g < c0 || g > c1 - 2) {  // split outside the chunk
@@ -620,16 +870,16 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             break;
         }
         const int k = g - c0, side = is_a ? 0 : 1;
-        s_lo[k][side] = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
-        s_hi[k][side] = make_float4(hi.x, hi.y, hi.z, __int_as_float(is_a ? l : r));
+        S.lo[k][side] = make_float4(lo.x, lo.y, lo.z, __int_as_float(link));
+        S.hi[k][side] = make_float4(hi.x, hi.y, hi.z, __int_as_float(is_a ? l : r));
         __threadfence_block();
-        if (atomicOr(&s_flag[k], 1u << side) == 0u) {  // first to arrive: the sibling may be in another chunk
+        if (atomicOr(&S.flag[k], 1u << side) == 0u) {  // first to arrive: the sibling may be in another chunk
             pend = g;
             break;
         }
         __threadfence_block();
         // second to arrive: the sibling's side of the slot is complete
-        const float4 olo = s_lo[k][side ^ 1], ohi = s_hi[k][side ^ 1];
+        const float4 olo = S.lo[k][side ^ 1], ohi = S.hi[k][side ^ 1];
         const int far = __float_as_int(ohi.w);
         if (is_a) {
             merge_ab(lo, hi, olo, ohi, lo, hi);
@@ -640,41 +890,41 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
         }
         link = g;
         if (l == 0 && r == n - 1) {
-            root->root = g;
-            root->top_lo = lo;
-            root->top_hi = hi;
+            A.root->root = g;
+            A.root->top_lo = lo;
+            A.root->top_hi = hi;
             break;
         }
     }
     __syncthreads();
-    if (i < n) {  // after the climbs: no global store is pending at their fences
-        leaves[2 * i] = tri_leaf[2 * t];
-        leaves[2 * i + 1] = tri_leaf[2 * t + 1];
+    if (i < n) {
+        A.leaves[2 * i] = __ldcg(A.tri_leaf + 2 * t);
+        A.leaves[2 * i + 1] = __ldcg(A.tri_leaf + 2 * t + 1);
     }
     // nodes of the chunk whose children both arrived here
     {
         const int g = c0 + tid;
-        if (g <= c1 - 2 && s_flag[tid] == 3u) {
-            const float4 alo = s_lo[tid][0], ahi = s_hi[tid][0], blo = s_lo[tid][1], bhi = s_hi[tid][1];
+        if (g <= c1 - 2 && S.flag[tid] == 3u) {
+            const float4 alo = S.lo[tid][0], ahi = S.hi[tid][0], blo = S.lo[tid][1], bhi = S.hi[tid][1];
             const int la = __float_as_int(ahi.w), rb = __float_as_int(bhi.w);
-            nodes[g].a_lo = alo;
-            nodes[g].a_hi = make_float4(ahi.x, ahi.y, ahi.z, __int_as_float(s_delta[la - c0]));
-            nodes[g].b_lo = blo;
-            nodes[g].b_hi = make_float4(bhi.x, bhi.y, bhi.z, __int_as_float(s_delta[rb - c0 + 1]));
-            range[g] = make_int2(la, rb);
+            A.nodes[g].a_lo = alo;
+            A.nodes[g].a_hi = make_float4(ahi.x, ahi.y, ahi.z, __int_as_float(S.delta[la - c0]));
+            A.nodes[g].b_lo = blo;
+            A.nodes[g].b_hi = make_float4(bhi.x, bhi.y, bhi.z, __int_as_float(S.delta[rb - c0 + 1]));
+            A.range[g] = make_int2(la, rb);
         }
     }
     // a climb that stopped at a node another chunk completes: its side, in the node
     {
         int g = out;
-        if (g < 0 && pend >= 0 && s_flag[pend - c0] != 3u) g = pend;
-        if (g >= 0) write_side(nodes, range, g, is_a, lo, hi, link, l, r, is_a ? dl : dr);
+        if (g < 0 && pend >= 0 && S.flag[pend - c0] != 3u) g = pend;
+        if (g >= 0) write_side(A.nodes, A.range, g, is_a, lo, hi, link, l, r, is_a ? dl : dr);
     }
     if (c0 < n) {
         // thread tid: boundary j = c0 + tid (delta dk, BIG_DELTA past the last boundary)
         // and leaf c0 + tid (its box, the identity box past the last leaf)
         const int j = c0 + tid;
-        const int dk = j <= n - 2 ? s_delta[tid + 1] : BIG_DELTA;
+        const int dk = j <= n - 2 ? S.delta[tid + 1] : BIG_DELTA;
         int pm = dk, sm = dk;  // inclusive prefix / suffix min over the warp
         float4 plo = leaf_lo, phi = leaf_hi, slo = leaf_lo, shi = leaf_hi;  // inclusive prefix / suffix unions
 #pragma unroll
@@ -692,32 +942,45 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             }
         }
         if (lane == 31) {
-            s_wmin[warp] = pm;
-            s_wlo[warp] = plo;
-            s_whi[warp] = phi;
+            S.wmin[warp] = pm;
+            S.wlo[warp] = plo;
+            S.whi[warp] = phi;
         }
         __syncthreads();
-        if (tid < W) {  // exclusive prefix / suffix over the warps, for warp tid
-            int a = BIG_DELTA, b = BIG_DELTA;
-            float4 al = ident_lo(), ah = ident_hi(), bl = ident_lo(), bh = ident_hi();
-            for (int w = 0; w < W; ++w) {
-                if (w < tid) {
-                    a = min(a, s_wmin[w]);
-                    box_union(al, ah, s_wlo[w], s_whi[w]);
-                } else if (w > tid) {
-                    b = min(b, s_wmin[w]);
-                    box_union(bl, bh, s_wlo[w], s_whi[w]);
+        if (warp == 0) {  // exclusive prefix / suffix over the warps, lane w for warp w
+            const bool in = lane < RW;
+            int a = in ? S.wmin[lane] : BIG_DELTA, b = a;  // inclusive scans, then shifted
+            float4 al = in ? S.wlo[lane] : ident_lo(), ah = in ? S.whi[lane] : ident_hi();
+            float4 bl = al, bh = ah;
+#pragma unroll
+            for (int o = 1; o < RW; o <<= 1) {
+                const int pa = __shfl_up_sync(0xffffffffu, a, o), pb = __shfl_down_sync(0xffffffffu, b, o);
+                const float4 pal = shfl_f4(al, o, true), pah = shfl_f4(ah, o, true);
+                const float4 pbl = shfl_f4(bl, o, false), pbh = shfl_f4(bh, o, false);
+                if (lane >= o) {
+                    a = min(a, pa);
+                    box_union(al, ah, pal, pah);
+                }
+                if (lane + o < RW) {
+                    b = min(b, pb);
+                    box_union(bl, bh, pbl, pbh);
                 }
             }
-            s_xpm[tid] = a;
-            s_xsm[tid] = b;
-            s_xplo[tid] = al;
-            s_xphi[tid] = ah;
-            s_xslo[tid] = bl;
-            s_xshi[tid] = bh;
+            // exclusive: the inclusive value of the neighbour (identity at the ends)
+            const int ea = __shfl_up_sync(0xffffffffu, a, 1), eb = __shfl_down_sync(0xffffffffu, b, 1);
+            const float4 eal = shfl_f4(al, 1, true), eah = shfl_f4(ah, 1, true);
+            const float4 ebl = shfl_f4(bl, 1, false), ebh = shfl_f4(bh, 1, false);
+            if (in) {
+                S.xpm[lane] = lane > 0 ? ea : BIG_DELTA;
+                S.xsm[lane] = lane + 1 < RW ? eb : BIG_DELTA;
+                S.xplo[lane] = lane > 0 ? eal : ident_lo();
+                S.xphi[lane] = lane > 0 ? eah : ident_hi();
+                S.xslo[lane] = lane + 1 < RW ? ebl : ident_lo();
+                S.xshi[lane] = lane + 1 < RW ? ebh : ident_hi();
+            }
         }
         __syncthreads();
-        const int wpm = s_xpm[warp], wsm = s_xsm[warp];
+        const int wpm = S.xpm[warp], wsm = S.xsm[warp];
         // strict prefix (suffix) minimum: delta below every delta to its left (right)
         // in the chunk
         const int ppm = __shfl_up_sync(0xffffffffu, pm, 1), nsm = __shfl_down_sync(0xffffffffu, sm, 1);
@@ -725,49 +988,55 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
         const int esm = min(wsm, lane < 31 ? nsm : BIG_DELTA);
         const bool pre = dk < epm, suf = dk < esm;
         // the chunk's leaves up to leaf j, and after it
-        float4 up_lo = s_xplo[warp], up_hi = s_xphi[warp];
+        float4 up_lo = S.xplo[warp], up_hi = S.xphi[warp];
         box_union(up_lo, up_hi, plo, phi);
-        float4 af_lo = s_xslo[warp], af_hi = s_xshi[warp];
+        float4 af_lo = S.xslo[warp], af_hi = S.xshi[warp];
         {
             const float4 nl = shfl_f4(slo, 1, false), nh = shfl_f4(shi, 1, false);
             if (lane < 31) box_union(af_lo, af_hi, nl, nh);
         }
         // node of boundary j spans chunks: no smaller delta on one side inside the chunk,
         // or j is the boundary to the next chunk
-        const bool span = j <= n - 2 && (j == c1 - 1 || (s_flag[tid] != 3u));
+        const bool span = j <= n - 2 && (j == c1 - 1 || (S.flag[tid] != 3u));
         const unsigned bs = __ballot_sync(0xffffffffu, suf), bp = __ballot_sync(0xffffffffu, pre);
         const unsigned bt = __ballot_sync(0xffffffffu, span);
         if (lane == 0) {
-            s_wsr[warp] = __popc(bs);
-            s_wpr[warp] = __popc(bp);
-            s_wtop[warp] = __popc(bt);
+            S.wsr[warp] = __popc(bs);
+            S.wpr[warp] = __popc(bp);
+            S.wtop[warp] = __popc(bt);
         }
         __syncthreads();
-        if (tid < W) {
-            int xs = 0, xp = 0, xt = 0, ts = 0, tp = 0, tt = 0;
-            for (int w = 0; w < W; ++w) {
-                if (w > tid) xs += s_wsr[w];
-                if (w < tid) {
-                    xp += s_wpr[w];
-                    xt += s_wtop[w];
+        if (warp == 0) {  // counts over the warps before / after warp `lane`, and in all
+            const bool in = lane < RW;
+            const int vs = in ? S.wsr[lane] : 0, vp = in ? S.wpr[lane] : 0, vt = in ? S.wtop[lane] : 0;
+            int is = vs, ip = vp, it = vt;  // inclusive prefix sums
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int qs = __shfl_up_sync(0xffffffffu, is, o), qp = __shfl_up_sync(0xffffffffu, ip, o);
+                const int qt = __shfl_up_sync(0xffffffffu, it, o);
+                if (lane >= o) {
+                    is += qs;
+                    ip += qp;
+                    it += qt;
                 }
-                ts += s_wsr[w];
-                tp += s_wpr[w];
-                tt += s_wtop[w];
             }
-            s_xos[tid] = xs;
-            s_xop[tid] = xp;
-            s_xot[tid] = xt;
-            if (tid == 0) {
-                s_nrec[0] = ts;
-                s_nrec[1] = tp;
-                s_nrec[2] = tt;
+            const int ts = __shfl_sync(0xffffffffu, is, 31), tp = __shfl_sync(0xffffffffu, ip, 31);
+            const int tt = __shfl_sync(0xffffffffu, it, 31);
+            if (in) {
+                S.xos[lane] = ts - is;  // suffix records after warp `lane`
+                S.xop[lane] = ip - vp;
+                S.xot[lane] = it - vt;
+            }
+            if (lane == 0) {
+                S.nrec[0] = ts;
+                S.nrec[1] = tp;
+                S.nrec[2] = tt;
             }
         }
         __syncthreads();
-        const int os = __popc(bs & ~((2u << lane) - 1u)) + s_xos[warp];
-        const int op = __popc(bp & ((1u << lane) - 1u)) + s_xop[warp];
-        const int ot = __popc(bt & ((1u << lane) - 1u)) + s_xot[warp];
+        const int os = __popc(bs & ~((2u << lane) - 1u)) + S.xos[warp];
+        const int op = __popc(bp & ((1u << lane) - 1u)) + S.xop[warp];
+        const int ot = __popc(bt & ((1u << lane) - 1u)) + S.xot[warp];
         if (suf && os < 32) {
             cv.srec[32 * chunk + os] = make_int2(j, dk);
             cv.sbox[2 * (32 * chunk + os)] = af_lo;
@@ -779,46 +1048,60 @@ k_build(const uint32_t* __restrict__ ucode, const uint32_t* __restrict__ utri, c
             cv.pbox[2 * (32 * chunk + op) + 1] = up_hi;
         }
         if (tid == BUILD_LEAVES - 1) {  // holds the whole chunk's prefix
-            cv.rcnt[3 * chunk] = min(s_nrec[0], 32);
-            cv.rcnt[3 * chunk + 1] = min(s_nrec[1], 32);
-            cv.rcnt[3 * chunk + 2] = min(s_nrec[2], 64);
+            cv.rcnt[3 * chunk] = min(S.nrec[0], 32);
+            cv.rcnt[3 * chunk + 1] = min(S.nrec[1], 32);
+            cv.rcnt[3 * chunk + 2] = min(S.nrec[2], 64);
             cv.cmin[chunk] = min(wpm, pm);
             cv.cbox[2 * chunk] = up_lo;
             cv.cbox[2 * chunk + 1] = up_hi;
         }
         if (span && ot < 64) cv.top[64 * chunk + ot] = make_int2(j, dk);  // at most 61 per chunk
     }
-    // the last CTA to finish sums the chunks up per 32, 1024 and 32768 chunks
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(cv.done, 1u) == gridDim.x - 1u;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
+    __syncthreads();  // the shared arrays are reused by the CTA's next chunk
+}
+
+// After chunk c's summary: the summaries per 32, 1024 and 32768 chunks.  Each entry
+// of level v counts its members as they finish (the CTA fences its writes, then
+// counts); the CTA that brings the count to the group's size reduces the group
+// into the level-v entry and counts that entry into level v + 1.
+__device__ void level_up(const RebuildArgs& A, int c, int n, int* s_last) {
+    const ChunkView& cv = A.cv;
+    const int lane = threadIdx.x & 31;
     int cnt[NLEV];
     level_counts(n, cnt);
+    int e = c;  // the finished entry of level v - 1
     for (int v = 1; v < NLEV; ++v) {
-        const int* mi = cv.cmin + cv.lev_off[v - 1];
-        const float4* bi = cv.cbox + 2 * cv.lev_off[v - 1];
-        for (int e = warp; e < cnt[v]; e += W) {
-            const int k = 32 * e + lane;
+        const int grp = e >> 5;
+        __threadfence();  // every thread's summary writes before the count
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t members = (uint32_t)min(32, cnt[v - 1] - 32 * grp);
+            *s_last = atomicAdd(A.gdone + cv.lev_off[v] + grp, 1u) == members - 1u ? 1 : 0;
+            __threadfence();  // the other members' writes before this CTA's reads
+        }
+        __syncthreads();
+        const bool last = *s_last != 0;
+        __syncthreads();  // s_last is rewritten on the next level
+        if (!last) return;
+        if (threadIdx.x < 32) {
+            const int k = 32 * grp + lane;
             int m = BIG_DELTA;
             float4 blo = ident_lo(), bhi = ident_hi();
             if (k < cnt[v - 1]) {
-                m = __ldcg(mi + k);
-                blo = __ldcg(bi + 2 * k);
-                bhi = __ldcg(bi + 2 * k + 1);
+                m = __ldcg(cv.cmin + cv.lev_off[v - 1] + k);
+                blo = __ldcg(cv.cbox + 2 * (cv.lev_off[v - 1] + k));
+                bhi = __ldcg(cv.cbox + 2 * (cv.lev_off[v - 1] + k) + 1);
             }
             warp_box_reduce(blo, bhi);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
             if (lane == 0) {
-                cv.cmin[cv.lev_off[v] + e] = m;
-                cv.cbox[2 * (cv.lev_off[v] + e)] = blo;
-                cv.cbox[2 * (cv.lev_off[v] + e) + 1] = bhi;
+                cv.cmin[cv.lev_off[v] + grp] = m;
+                cv.cbox[2 * (cv.lev_off[v] + grp)] = blo;
+                cv.cbox[2 * (cv.lev_off[v] + grp) + 1] = bhi;
             }
         }
-        __syncthreads();
+        e = grp;
     }
 }
 
@@ -831,13 +1114,13 @@ __device__ int nearest_chunk(const ChunkView& cv, const int cnt[NLEV], int c, in
     for (int v = 0; v < NLEV; ++v) {
         const int* m = cv.cmin + cv.lev_off[v];
         const int base = idx & ~31, e = base + lane;
-        const bool hit = (right ? e > idx : e < idx) && e < cnt[v] && __ldg(m + e) < d;
+        const bool hit = (right ? e > idx : e < idx) && e < cnt[v] && __ldcg(m + e) < d;
         unsigned b = __ballot_sync(0xffffffffu, hit);
         if (b) {
             int f = right ? base + __ffs(b) - 1 : base + 31 - __clz(b);
             for (int u = v - 1; u >= 0; --u) {  // descend: the first qualifying entry of group f
                 const int b2 = 32 * f, e2 = b2 + lane;
-                const bool h2 = e2 < cnt[u] && __ldg(cv.cmin + cv.lev_off[u] + e2) < d;
+                const bool h2 = e2 < cnt[u] && __ldcg(cv.cmin + cv.lev_off[u] + e2) < d;
                 b = __ballot_sync(0xffffffffu, h2);
                 if (!b) {  // the group's min said otherwise: corrupt summaries
                     if (lane == 0) atomicOr(err, ERR_TIMEOUT);
@@ -857,7 +1140,7 @@ __device__ int nearest_chunk(const ChunkView& cv, const int cnt[NLEV], int c, in
 // left of g (right of g, with right); g < 0: any position.  -1: none.
 __device__ __forceinline__ int first_record(const int2* rec, int count, int g, int d, bool right, int lane,
                                             int2& out) {
-    const int2 q = lane < count ? __ldg(rec + lane) : make_int2(0, BIG_DELTA);
+    const int2 q = lane < count ? __ldcg(rec + lane) : make_int2(0, BIG_DELTA);
     const bool hit = lane < count && q.y < d && (g < 0 || (right ? q.x > g : q.x < g));
     const unsigned b = __ballot_sync(0xffffffffu, hit);
     if (!b) return -1;
@@ -873,12 +1156,12 @@ __device__ void chunk_union(const ChunkView& cv, const int cnt[NLEV], int a, int
     for (int v = 0; v < NLEV && a <= b; ++v) {
         const float4* bx = cv.cbox + 2 * cv.lev_off[v];
         if ((a >> 5) == (b >> 5) || v == NLEV - 1) {
-            for (int e = a + lane; e <= b; e += 32) box_union(ul, uh, __ldg(bx + 2 * e), __ldg(bx + 2 * e + 1));
+            for (int e = a + lane; e <= b; e += 32) box_union(ul, uh, __ldcg(bx + 2 * e), __ldcg(bx + 2 * e + 1));
             break;
         }
         const int e1 = a + lane, e2 = (b & ~31) + lane;
-        if (e1 <= (a | 31)) box_union(ul, uh, __ldg(bx + 2 * e1), __ldg(bx + 2 * e1 + 1));
-        if (e2 <= b) box_union(ul, uh, __ldg(bx + 2 * e2), __ldg(bx + 2 * e2 + 1));
+        if (e1 <= (a | 31)) box_union(ul, uh, __ldcg(bx + 2 * e1), __ldcg(bx + 2 * e1 + 1));
+        if (e2 <= b) box_union(ul, uh, __ldcg(bx + 2 * e2), __ldcg(bx + 2 * e2 + 1));
         a = (a >> 5) + 1;
         b = (b >> 5) - 1;
     }
@@ -891,76 +1174,192 @@ __device__ void chunk_union(const ChunkView& cv, const int cnt[NLEV], int a, int
 // suffix / prefix record past the node with a smaller delta, in the node's chunk or
 // in the nearest chunk with a smaller min), the box is the union of the leaf boxes in
 // the range (the records' partial unions and whole chunks between), and the node
-// enters its parent (the range end with the larger delta) as build_internal's climb
-// would have put it there.
-constexpr int TOP_WARPS = 8;
-__global__ void __launch_bounds__(TOP_WARPS * 32)
-k_build_top(ChunkView cv, Node* nodes, int2* range, BvhRoot* root, int* err) {
-    const int nt = root->n_tris;
-    const int n = min(root->n_leaves, nt);
+// enters its parent (the range end with the larger delta) as the climb would have
+// put it there.
+__device__ void phase_top(const RebuildArgs& A, int n) {
+    const ChunkView& cv = A.cv;
     int cnt[NLEV];
     level_counts(n, cnt);
     const int lane = (int)(threadIdx.x & 31u);
     // each chunk's nodes that span chunks sit in its 64 slots; iteration `it` takes slot
     // it / F of chunk it % F, so the (few, low) occupied slots spread over all warps
     const uint32_t F = (uint32_t)cnt[0], slots = 64u * F;
-    const uint32_t nw = gridDim.x * TOP_WARPS;
-    for (uint32_t it = blockIdx.x * TOP_WARPS + (threadIdx.x >> 5); it < slots; it += nw) {
+    const uint32_t nw = gridDim.x * RW;
+    for (uint32_t it = blockIdx.x * RW + (threadIdx.x >> 5); it < slots; it += nw) {
         const uint32_t ch = it % F, sl = it / F;
-        if ((int)sl >= __ldg(cv.rcnt + 3 * ch + 2)) continue;
-        const int2 item = __ldg(cv.top + 64 * ch + sl);
+        if ((int)sl >= __ldcg(cv.rcnt + 3 * ch + 2)) continue;
+        const int2 item = __ldcg(cv.top + 64 * ch + sl);
         const int g = item.x, d = item.y, c = g / BUILD_LEAVES;
         if (g < 0 || g > n - 2 || c >= cnt[0]) {
-            if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+            if (lane == 0) atomicOr(A.err, ERR_TIMEOUT);
             continue;
         }
         // left end: boundary jl (leaves from jl + 1), -1 = none
         int2 q;
         int jl = -1, dlft = -1, cl = -1;
         float4 lo = ident_lo(), hi = ident_hi();
-        int k = first_record(cv.srec + 32 * c, __ldg(cv.rcnt + 3 * c), g, d, false, lane, q);
+        int k = first_record(cv.srec + 32 * c, __ldcg(cv.rcnt + 3 * c), g, d, false, lane, q);
         int cc = c;
         if (k < 0) {
-            cc = nearest_chunk(cv, cnt, c, d, false, lane, err);
-            if (cc >= 0) k = first_record(cv.srec + 32 * cc, __ldg(cv.rcnt + 3 * cc), -1, d, false, lane, q);
+            cc = nearest_chunk(cv, cnt, c, d, false, lane, A.err);
+            if (cc >= 0) k = first_record(cv.srec + 32 * cc, __ldcg(cv.rcnt + 3 * cc), -1, d, false, lane, q);
         }
         if (k >= 0) {
             jl = q.x;
             dlft = q.y;
             cl = cc;
-            box_union(lo, hi, __ldg(cv.sbox + 2 * (32 * cc + k)), __ldg(cv.sbox + 2 * (32 * cc + k) + 1));
+            box_union(lo, hi, __ldcg(cv.sbox + 2 * (32 * cc + k)), __ldcg(cv.sbox + 2 * (32 * cc + k) + 1));
         }
         // right end: boundary jr (leaves up to jr), n - 1 = none
         int jr = n - 1, drgt = -1, cr = cnt[0] - 1;
-        k = first_record(cv.prec + 32 * c, __ldg(cv.rcnt + 3 * c + 1), g, d, true, lane, q);
+        k = first_record(cv.prec + 32 * c, __ldcg(cv.rcnt + 3 * c + 1), g, d, true, lane, q);
         cc = c;
         if (k < 0) {
-            cc = nearest_chunk(cv, cnt, c, d, true, lane, err);
-            if (cc >= 0) k = first_record(cv.prec + 32 * cc, __ldg(cv.rcnt + 3 * cc + 1), -1, d, true, lane, q);
+            cc = nearest_chunk(cv, cnt, c, d, true, lane, A.err);
+            if (cc >= 0) k = first_record(cv.prec + 32 * cc, __ldcg(cv.rcnt + 3 * cc + 1), -1, d, true, lane, q);
         }
         if (k >= 0) {
             jr = q.x;
             drgt = q.y;
             cr = cc;
-            box_union(lo, hi, __ldg(cv.pbox + 2 * (32 * cc + k)), __ldg(cv.pbox + 2 * (32 * cc + k) + 1));
+            box_union(lo, hi, __ldcg(cv.pbox + 2 * (32 * cc + k)), __ldcg(cv.pbox + 2 * (32 * cc + k) + 1));
         } else {
-            box_union(lo, hi, __ldg(cv.cbox + 2 * cr), __ldg(cv.cbox + 2 * cr + 1));  // the last chunk
+            box_union(lo, hi, __ldcg(cv.cbox + 2 * cr), __ldcg(cv.cbox + 2 * cr + 1));  // the last chunk
         }
         chunk_union(cv, cnt, cl + 1, cr - 1, lane, lo, hi);
         if (lane == 0) {
             if (jl < 0 && jr == n - 1) {
-                root->root = g;
-                root->top_lo = lo;
-                root->top_hi = hi;
+                A.root->root = g;
+                A.root->top_lo = lo;
+                A.root->top_hi = hi;
             } else {
                 const bool is_a = drgt > dlft;
-                write_side(nodes, range, is_a ? jr : jl, is_a, lo, hi, g, jl + 1, jr, is_a ? dlft : drgt);
+                write_side(A.nodes, A.range, is_a ? jr : jl, is_a, lo, hi, g, jl + 1, jr, is_a ? dlft : drgt);
             }
         }
     }
 }
 
+// ---- the launch -----------------------------------------------------------------------------------
+__global__ void __launch_bounds__(RB, 2) k_rebuild(const RebuildArgs A) {
+    extern __shared__ __align__(16) unsigned char rb_smem[];
+    __shared__ uint32_t s_scan[32];
+    __shared__ float s_red[6 * RW];
+    __shared__ float s_frame[8];
+    __shared__ int s_ok, s_claim;
+    uint32_t target = 0;
+    const int nt = A.nt;
+    // the last build's sorted list (keys[cur], vals[cur]) and codes are usable: read
+    // before any CTA can change the root record
+    const bool coherent = A.coherent && ld_volatile(reinterpret_cast<const uint32_t*>(&A.root->perm_valid)) != 0u;
+    const int cur = coherent ? (int)ld_volatile(reinterpret_cast<const uint32_t*>(&A.root->sorted)) & 1 : 1;
+    const int n_prev = A.root->n_leaves;
+    // what the later phases need at zero (read only after the next barrier)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        A.chg[0] = 0u;
+        A.root->n_tris = nt;
+    }
+    {
+        const size_t zw = (size_t)PASSES * RADIX + (size_t)PASSES * A.tiles_sort * RADIX + PASSES;
+        for (size_t k = (size_t)blockIdx.x * RB + threadIdx.x; k < zw; k += (size_t)gridDim.x * RB) A.ghist[k] = 0u;
+        for (int k = blockIdx.x * RB + threadIdx.x; k < A.n_entries; k += gridDim.x * RB) A.gdone[k] = 0u;
+    }
+    phase_verts(A);
+    bool ok = grid_barrier(A.sync, target, true, A.err, &s_ok);
+    if (ok) phase_boxes(A, s_red);
+    ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+    if (ok) phase_codes(A, coherent, s_red, s_frame);
+    ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+    // the sort: same decision in every CTA (from words complete at the barrier)
+    const uint32_t nchg = ld_volatile(A.chg);
+    const bool merge = coherent && nchg <= (uint32_t)CHG_CAP;
+    int after = cur;  // buffer holding this build's sorted list
+    bool fresh = true;  // the sorted list changed: de-duplicate it again
+    if (merge) {
+        if (nchg == 0u) {
+            fresh = false;  // every code as before: the last build's list and leaves stand
+        } else {
+            after = cur ^ 1;
+            if (ok)
+                phase_merge(A, (int)nchg, A.keys[cur], A.vals[cur], A.keys[after], A.vals[after],
+                            *reinterpret_cast<MergeSmem*>(rb_smem));
+            ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+        }
+    } else {
+        if (ok) phase_hist(A, reinterpret_cast<uint32_t*>(rb_smem));
+        ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+        for (int p = 0; p < PASSES; ++p) {
+            if (ok) phase_sort_pass(A, p, *reinterpret_cast<SortSmem*>(rb_smem), s_scan, &s_claim);
+            ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+        }
+        after = (PASSES - 1) & 1;
+    }
+    int n = n_prev;
+    if (fresh) {
+        if (ok) phase_unique_count(A, A.keys[after], s_scan);
+        ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+        if (ok) n = phase_unique_write(A, A.keys[after], A.vals[after], s_scan);
+        ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // the sort buffers now hold this build's list, unless some wait gave up
+        const bool bad = !ok || (ld_volatile(reinterpret_cast<const uint32_t*>(A.err)) & ERR_TIMEOUT) != 0u;
+        A.root->perm_valid = bad ? 0 : 1;
+        A.root->sorted = after;
+    }
+    n = min(n, nt);
+    const int chunks = (n + BUILD_LEAVES - 1) / BUILD_LEAVES;
+    if (ok)
+        for (int c = blockIdx.x; c < chunks; c += gridDim.x) {
+            build_chunk(A, c, n, *reinterpret_cast<BuildSmem*>(rb_smem));
+            level_up(A, c, n, &s_claim);
+        }
+    ok = grid_barrier(A.sync, target, ok, A.err, &s_ok);
+    if (ok) phase_top(A, n);
+    // the last CTA out leaves both counters at zero for the next launch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(A.sync + 1, 1u) == gridDim.x - 1u) {
+            atomicExch(A.sync, 0u);
+            atomicExch(A.sync + 1, 0u);
+        }
+    }
+}
+
+// Self-test of the grid barrier's bounded wait: one CTA waits for an arrival count
+// that no other CTA will bring; the wait gives up after kGridWaitNs, records
+// ERR_TIMEOUT and returns.
+__global__ void k_selftest_grid_wait(uint32_t* ctr, int* err) {
+    __shared__ int s_ok;
+    uint32_t target = 1;  // as if one barrier of this one-CTA launch had passed
+    (void)grid_barrier(ctr, target, true, err, &s_ok);
+}
+
+// Self-test of the look-back's bounded wait: one thread looks back from tile 1 at a
+// status word (tile 0's) that nothing publishes; the walk gives up after SPIN_LIMIT
+// sleeps, records ERR_TIMEOUT and returns.
+__global__ void k_selftest_look_back(const uint32_t* status, int* err) {
+    if (threadIdx.x == 0) (void)look_back(status, 1, 1, err);
+}
+
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// CTAs of k_rebuild that fit on the device at once (cooperative launch limit)
+int resident_ctas() {
+    static std::mutex mu;
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!cached[dev]) {
+        int sms = 0, per = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild, RB, kSmemBytes) != cudaSuccess) return 0;
+        cached[dev] = sms * per;
+    }
+    return cached[dev];
+}
 
 }  // namespace
 
@@ -969,6 +1368,7 @@ void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
     nt = nt_;
     has_normals = normals;
     tiles_sort = nt > 0 ? cdiv(nt, SORT_TILE) : 0;
+    max_ctas = std::max(1, cdiv(std::max(nt, 1), RB));
     int ni = nt > 1 ? nt - 1 : 1;
     a.want(&xyz_in, (size_t)nv * 3 + 4);
     a.want(&nrm_in, (size_t)nv * 3 + 4);
@@ -1002,63 +1402,74 @@ void BvhBuffers::plan(Arena& a, int nv_, int nt_, bool normals) {
     a.want(&rcnt, 3 * (size_t)chunks);
     a.want(&top, 64 * (size_t)chunks);
     a.want(&root, 1);
-    // histograms | sort status (PASSES x tiles x RADIX) | sort counters | unique status | unique counter
-    // | rebuild mode word | finished chunk CTAs
-    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES + tiles_sort + 3;
+    // histograms | sort status (PASSES x tiles x RADIX) | sort counters (the launch
+    // clears them) | CTA box unions | CTA leaf counts | change list | barrier counters
+    scratch_words = (size_t)PASSES * RADIX + (size_t)PASSES * tiles_sort * RADIX + PASSES;
     a.want(&scratch, scratch_words);
+    a.want(&part, 8 * (size_t)max_ctas);
+    a.want(&ucnt, (size_t)max_ctas);
+    a.want(&chg, 1 + 3 * (size_t)CHG_CAP);
+    a.want(&sync, 2);
+    n_entries = entries;
+    a.want(&gdone, (size_t)entries);
 }
 
-namespace {
-// Self-test of the look-back's bounded wait: one thread looks back from tile 1 at a
-// status word (tile 0's) that nothing publishes; the walk gives up after SPIN_LIMIT
-// sleeps, records ERR_TIMEOUT and returns.
-__global__ void k_selftest_look_back(const uint32_t* status, int* err) {
-    if (threadIdx.x == 0) (void)look_back(status, 1, 1, err);
+cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s, const float* xyz,
+                       const float* nrm, float4* margin_state, int64_t m0, int64_t m1) {
+    if (b.nt == 0) return cudaSuccess;
+    const int res = resident_ctas();
+    if (res <= 0) return cudaErrorLaunchOutOfResources;
+    RebuildArgs A;
+    A.xyz = xyz ? xyz : b.xyz_in;
+    A.nrm = b.has_normals ? (xyz ? nrm : b.nrm_in) : nullptr;
+    A.margin_state = margin_state;
+    A.m0 = m0;
+    A.m1 = m1;
+    A.tris = b.tris;
+    A.nv = b.nv;
+    A.nt = b.nt;
+    A.thickness = thickness;
+    A.depth = box_depth;
+    A.coherent = b.coherent ? 1 : 0;
+    A.tiles_sort = b.tiles_sort;
+    A.verts = b.verts;
+    A.tri_box = b.tri_box;
+    A.tri_leaf = b.tri_leaf;
+    A.codes = b.codes;
+    for (int k = 0; k < 2; ++k) {
+        A.keys[k] = b.keys[k];
+        A.vals[k] = b.vals[k];
+    }
+    A.ucode = b.ucode;
+    A.utri = b.utri;
+    A.nodes = b.nodes;
+    A.leaves = b.leaves;
+    A.range = b.range;
+    A.root = b.root;
+    A.cv = ChunkView{b.cmin, b.cbox, b.srec, b.sbox, b.prec, b.pbox, b.rcnt, b.top,
+                     {b.lev_off[0], b.lev_off[1], b.lev_off[2], b.lev_off[3]}};
+    A.ghist = b.scratch;
+    A.sstat = A.ghist + PASSES * RADIX;
+    A.scount = A.sstat + (size_t)PASSES * b.tiles_sort * RADIX;
+    A.part = b.part;
+    A.ucnt = b.ucnt;
+    A.chg = b.chg;
+    A.sync = b.sync;
+    A.gdone = b.gdone;
+    A.n_entries = b.n_entries;
+    A.err = d_err;
+    const int grid = std::min(res, b.max_ctas);
+    void* args[] = {&A};
+    return cudaLaunchCooperativeKernel((const void*)k_rebuild, dim3(grid), dim3(RB), args, kSmemBytes, s);
 }
-}  // namespace
 
 cudaError_t launch_selftest_look_back(const uint32_t* zero_status, int* err, cudaStream_t s) {
     k_selftest_look_back<<<1, 32, 0, s>>>(zero_status, err);
     return cudaGetLastError();
 }
 
-cudaError_t lbvh_build(BvhBuffers& b, float thickness, float box_depth, int* d_err, cudaStream_t s) {
-    if (b.nt == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(b.scratch, 0, b.scratch_words * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    uint32_t* ghist = b.scratch;
-    uint32_t* sstat = ghist + PASSES * RADIX;
-    uint32_t* scount = sstat + (size_t)PASSES * b.tiles_sort * RADIX;
-    uint32_t* ustat = scount + PASSES;
-    uint32_t* ucount = ustat + b.tiles_sort;
-    uint32_t* mode = ucount + 1;
-    ChunkView cv{b.cmin, b.cbox, b.srec, b.sbox, b.prec, b.pbox, b.rcnt, b.top, mode + 1,
-                 {b.lev_off[0], b.lev_off[1], b.lev_off[2], b.lev_off[3]}};
-    k_body_prep<<<cdiv(b.nv, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.xyz_in, b.has_normals ? b.nrm_in : nullptr,
-                                                                     b.nv, thickness, b.verts, b.root, b.nt);
-    k_tri_boxes<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.verts, b.nv, b.tris, b.nt, box_depth, b.tri_box,
-                                                                     b.tri_leaf, b.root, d_err);
-    k_morton<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.tri_box, b.nt, b.root, b.codes, ghist);
-    if (b.coherent)
-        k_coherence<<<cdiv(b.nt, BUILD_THREADS), BUILD_THREADS, 0, s>>>(b.codes, b.keys[1], b.vals[1], b.nt, b.root,
-                                                                         mode);
-    const uint32_t* kin = b.codes;
-    const uint32_t* vin = nullptr;
-    for (int p = 0; p < PASSES; ++p) {
-        uint32_t* ko = b.keys[p & 1];
-        uint32_t* vo = b.vals[p & 1];
-        k_sort_pass<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, ko, vo, b.nt, 8 * p, ghist + p * RADIX,
-                                                          sstat + (size_t)p * b.tiles_sort * RADIX, scount + p, mode, d_err);
-        kin = ko;
-        vin = vo;
-    }
-    k_unique<<<b.tiles_sort, SORT_THREADS, 0, s>>>(kin, vin, b.nt, b.ucode, b.utri, ustat, ucount, b.tiles_sort,
-                                                   b.root, mode, d_err);
-    k_build<<<b.chunks, BUILD_LEAVES, 0, s>>>(b.ucode, b.utri, b.tri_box, b.tri_leaf, b.nodes, b.leaves, b.range,
-                                               b.root, cv, d_err);
-    if (b.chunks > 1)  // else the whole tree is one chunk's
-        k_build_top<<<std::min(cdiv(64 * b.chunks, TOP_WARPS), 1024), TOP_WARPS * 32, 0, s>>>(cv, b.nodes, b.range,
-                                                                                              b.root, d_err);
+cudaError_t launch_selftest_grid_wait(uint32_t* zero_counter, int* err, cudaStream_t s) {
+    k_selftest_grid_wait<<<1, 32, 0, s>>>(zero_counter, err);
     return cudaGetLastError();
 }
 

@@ -145,9 +145,11 @@ extern "C" int visg_lbvh_build_noalloc(const float* d_xyz, const float* d_normal
     b.ucode = d_sorted_codes;
     b.utri = reinterpret_cast<uint32_t*>(d_sorted_tris);
 
-    // what must start at zero: the error word (the build clears its histograms,
-    // look-back status words and counters itself)
+    // what must start at zero: the error word and the build's grid-barrier counters
+    // (the array holds the last call's data, laid out for its sizes); the build
+    // clears its histograms, look-back status words and tile counters itself
     cudaError_t e = cudaMemsetAsync(d_err, 0, 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.sync, 0, 2 * sizeof(uint32_t), s);
     if (e == cudaSuccess) e = lbvh_build(b, thickness, box_depth, d_err, s);
     if (e == cudaSuccess && n_tris > 1) {
         const unsigned grid = (unsigned)((n_tris + 255) / 256);

@@ -67,8 +67,9 @@ def test_oracle_lbvh_dedupe_keeps_lowest_index(n, dup):
 
 
 def bottom_up_build(codes: np.ndarray, seed: int = 0):
-    """The device build (visg_lbvh.cu k_build), executed leaf by leaf in a random
-    order: climb while the parent has already been reached by the other child.
+    """The device build's chunk climb (visg_lbvh.cu build_chunk), executed leaf by
+    leaf in a random order: climb while the parent has already been reached by the
+    other child.
     Returns (links A/B per split node, ranges, root split)."""
     n = len(codes)
     rng = np.random.default_rng(seed)
@@ -138,6 +139,57 @@ def test_bottom_up_build_equals_karras(n, seed):
         assert rl[root] == 0 and rr[root] == len(codes) - 1
         ca, cb = renumber(la, lb, rl, rr, root)
         assert np.array_equal(ca, b["child_a"]) and np.array_equal(cb, b["child_b"])
+
+
+def incremental_merge(old_codes: np.ndarray, new_codes: np.ndarray) -> np.ndarray:
+    """The rebuild's merge path (visg_lbvh.cu phase_merge), restated: the last build's
+    list sorted by (old code, triangle), the triangles whose code changed sorted by
+    (new code, triangle) and by (old code, triangle), and each entry's new position
+    from lower bounds into those two arrays.  Returns the keys (code << 32 |
+    triangle) by position, each position written once."""
+    nt = len(old_codes)
+    tri = np.arange(nt, dtype=np.uint64)
+    old_list = np.sort((old_codes.astype(np.uint64) << np.uint64(32)) | tri)
+    chg = np.nonzero(new_codes != old_codes)[0]
+    nc = len(chg)
+    knew = np.sort((new_codes[chg].astype(np.uint64) << np.uint64(32)) | tri[chg])
+    kold = np.sort((old_codes[chg].astype(np.uint64) << np.uint64(32)) | tri[chg])
+    below = lambda a, x: int(np.searchsorted(a, x, side="left"))  # entries of a below x
+    out = np.zeros(nt, np.uint64)
+    hits = np.zeros(nt, np.int64)
+    for j in range(below(knew, old_list[0])):  # changed entries below the first old key
+        out[j] = knew[j]
+        hits[j] += 1
+    for s in range(nt):
+        ks = old_list[s]
+        q, r = below(kold, ks), below(knew, ks)
+        if not (q < nc and kold[q] == ks):  # unchanged: keeps its place among the others
+            out[s - q + r] = ks
+            hits[s - q + r] += 1
+        r1, q1 = (below(knew, old_list[s + 1]), below(kold, old_list[s + 1])) if s + 1 < nt else (nc, nc)
+        for j in range(r, r1):  # changed entries between old slots s and s + 1
+            out[j + s + 1 - q1] = knew[j]
+            hits[j + s + 1 - q1] += 1
+    assert (hits == 1).all()
+    return out
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_incremental_merge_equals_a_full_sort(seed):
+    """The merge that replaces the radix sort when few Morton codes changed gives the
+    stable (code, triangle) order of the new codes: random code sets with many
+    duplicates, with none, some and all of the codes changed."""
+    rng = np.random.default_rng(seed)
+    for _ in range(100):
+        nt = int(rng.integers(1, 80))
+        old = rng.integers(0, int(rng.integers(1, 40)), nt).astype(np.uint32)
+        new = old.copy()
+        k = int(rng.integers(0, nt + 1)) if rng.random() < 0.8 else nt
+        idx = rng.choice(nt, size=k, replace=False)
+        new[idx] = rng.integers(0, 40, k).astype(np.uint32)
+        tri = np.arange(nt, dtype=np.uint64)
+        full = np.sort((new.astype(np.uint64) << np.uint64(32)) | tri)
+        assert np.array_equal(incremental_merge(old, new), full)
 
 
 def test_query_matches_manual_first_hit():

@@ -130,6 +130,30 @@ def test_lbvh_coherent_rebuilds_match_oracle():
     assert n_leaves[0] == 300 and n_leaves[2] == 299 and n_leaves[4] == 300
 
 
+def test_lbvh_merge_and_radix_rebuilds_alternate():
+    """Rebuilds of a 20,000-triangle soup alternate between the two sorts: a small
+    jitter changes fewer than 2,048 codes (the merge into the last build's order),
+    a large one more (the four radix passes), and the merge then starts from the
+    order the radix passes left.  Every build equals the oracle's."""
+    xyz, tris = soup(20000, seed=7, dup_frac=0.05)
+    g, o = lbvh_pair(xyz, tris)
+    rng = np.random.default_rng(8)
+    last = o.export_lbvh()["tri_codes"]
+    changed = []
+    p = xyz
+    for k, sigma in enumerate((2e-6, 2e-2, 2e-6, 0.0, 3e-2, 2e-6)):  # each from the last positions
+        p = (p + rng.normal(0.0, sigma, xyz.shape)).astype(np.float32) if sigma else p
+        g.update_body(p, None)
+        o.update_body(p, None)
+        a, r = g.export_lbvh(), o.export_lbvh()
+        assert lbvh_diff(a, r) == [], k
+        changed.append(int((r["tri_codes"] != last).sum()))
+        last = r["tri_codes"]
+    print("codes changed per rebuild", changed)
+    assert 0 < changed[0] < 2048 and changed[1] > 2048 and 0 < changed[2] < 2048 and changed[4] > 2048
+    assert changed[3] == 0 and 0 < changed[5] < 2048
+
+
 @pytest.mark.parametrize("name", ["ico3_noise", "capsules"])
 def test_first_hit_queries_match_oracle(name):
     b = BODIES[name]()
@@ -723,10 +747,10 @@ def test_packed_square_root_and_reciprocal_equal_the_intrinsics_on_every_float()
 
 
 def test_bounded_waits_give_up_and_leave_the_device_usable():
-    """Failure detection without a fault: a staging-ring wait and a radix look-back
-    wait that nothing completes give up (bounded), report ERR_TIMEOUT, and the
-    simulator works normally afterwards."""
-    assert vs.selftest_bounded_waits() == 3
+    """Failure detection without a fault: a staging-ring wait, a radix look-back wait
+    and an LBVH grid-barrier wait that nothing completes give up (bounded), report
+    ERR_TIMEOUT, and the simulator works normally afterwards."""
+    assert vs.selftest_bounded_waits() == 7
     cloth, cl, body, p = ref_scene(side=16, subdiv=2)
     g, o = run_pair(cloth, cl, body, p, 20)
     assert_state_equal(g, o)
