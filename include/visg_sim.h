@@ -291,8 +291,8 @@ int visg_batch_update_body(VisgBatch* b, int32_t garment, const float* body_xyz,
  * and keeps the fastest; *block and *ctas_per_sm (may be NULL) report the choice.
  * Leaves the simulation state unchanged. */
 int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm);
-/* Sets the step kernel's launch shape directly (no timing): block = 128, 256 or
- * 512 vertices per tile; ctas_per_sm = persistent CTAs per SM (1 .. what fits), or
+/* Sets the step kernel's launch shape directly (no timing): block = 128, 256, 512
+ * or 1024 vertices per tile; ctas_per_sm = persistent CTAs per SM (1 .. what fits), or
  * 0 for one CTA per tile.  For reproducible timings and for callers that tune
  * offline.  No counterpart in the reference (it launches one fixed shape). */
 int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas_per_sm);

@@ -50,11 +50,17 @@ int cuda_fail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
-constexpr int kBlocks[3] = {128, 256, 512};
+constexpr int kNumBlocks = 4;
+constexpr int kBlocks[kNumBlocks] = {128, 256, 512, 1024};
 // largest sliced-ELL block (entries) a tile of each block size may stage in shared
-// memory: 16 entries per vertex; two buffers take 32 / 64 / 128 KB
-constexpr int kStageCap[3] = {2048, 4096, 8192};
-int block_index(int b) { return b == 128 ? 0 : (b == 256 ? 1 : (b == 512 ? 2 : -1)); }
+// memory: 16 entries per vertex (14 for 1024, whose two buffers must fit the 227 KB a
+// CTA may hold); two buffers take 32 / 64 / 128 / 224 KB
+constexpr int kStageCap[kNumBlocks] = {2048, 4096, 8192, 14336};
+int block_index(int b) {
+    for (int i = 0; i < kNumBlocks; ++i)
+        if (kBlocks[i] == b) return i;
+    return -1;
+}
 
 struct GarmentIn {
     std::vector<float> xyz;
@@ -116,7 +122,7 @@ struct Engine {
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, fork2 = nullptr, join2 = nullptr;
     // garment groups stepped as independent chains: group 1 starts at garment
     // boundary vsplit (vertex), i.e. at tile tsplit[b] of each tile table
-    int tsplit[3] = {0, 0, 0};
+    int tsplit[kNumBlocks] = {0, 0, 0, 0};
     int64_t vsplit = 0;
     bool finalized = false;
     std::vector<GarmentIn> gin;
@@ -132,10 +138,10 @@ struct Engine {
     uint32_t* d_rowp = nullptr;
     uint2* d_ent = nullptr;
     float* d_k = nullptr;
-    int4* d_tiles[3] = {nullptr, nullptr, nullptr};
-    int n_tiles[3] = {0, 0, 0};
-    int2* d_twin[3] = {nullptr, nullptr, nullptr};  // per tile sliced-ELL block {first entry, count}
-    int win_cap[3] = {0, 0, 0};                      // entries per stage buffer, 0 = no tile staged
+    int4* d_tiles[kNumBlocks] = {nullptr, nullptr, nullptr, nullptr};
+    int n_tiles[kNumBlocks] = {0, 0, 0, 0};
+    int2* d_twin[kNumBlocks] = {nullptr, nullptr, nullptr, nullptr};  // per tile sliced-ELL block {first entry, count}
+    int win_cap[kNumBlocks] = {0, 0, 0, 0};                           // entries per stage buffer, 0 = no tile staged
     uint2* d_sell = nullptr;                         // sliced-ELL springs
     float* d_sellk = nullptr;
     uint32_t* d_slice_off = nullptr;
@@ -385,9 +391,9 @@ struct Engine {
                 }
             }
         // tiles for each block size, with the sliced-ELL block of each one's slices
-        std::vector<std::vector<int4>> tiles(3);
-        std::vector<std::vector<int2>> twin(3);
-        for (int b = 0; b < 3; ++b) {
+        std::vector<std::vector<int4>> tiles(kNumBlocks);
+        std::vector<std::vector<int2>> twin(kNumBlocks);
+        for (int b = 0; b < kNumBlocks; ++b) {
             const int cap = kStageCap[b];
             win_cap[b] = 0;
             for (int g = 0; g < G; ++g)
@@ -410,7 +416,7 @@ struct Engine {
             for (int g = 2; g < G; ++g)
                 if (std::llabs(2 * voff[g] - N) < std::llabs(2 * voff[gs] - N)) gs = g;
             vsplit = voff[gs];
-            for (int b = 0; b < 3; ++b) {
+            for (int b = 0; b < kNumBlocks; ++b) {
                 tsplit[b] = 0;
                 while (tsplit[b] < (int)tiles[b].size() && tiles[b][tsplit[b]].x < gs) ++tsplit[b];
             }
@@ -422,7 +428,7 @@ struct Engine {
         arena.want(&d_rowp, (size_t)N + 2);
         arena.want(&d_ent, (size_t)E + 1);
         if (perk) arena.want(&d_k, (size_t)E + 1);
-        for (int b = 0; b < 3; ++b) {
+        for (int b = 0; b < kNumBlocks; ++b) {
             n_tiles[b] = (int)tiles[b].size();
             arena.want(&d_tiles[b], tiles[b].size() + 1);
             arena.want(&d_twin[b], twin[b].size() + 1);
@@ -462,7 +468,7 @@ struct Engine {
         CU(cudaMemcpy(d_rowp, h_rowp.data(), h_rowp.size() * 4, cudaMemcpyHostToDevice));
         if (E > 0) CU(cudaMemcpy(d_ent, ent.data(), E * sizeof(uint2), cudaMemcpyHostToDevice));
         if (perk && E > 0) CU(cudaMemcpy(d_k, kk.data(), E * sizeof(float), cudaMemcpyHostToDevice));
-        for (int b = 0; b < 3; ++b) {
+        for (int b = 0; b < kNumBlocks; ++b) {
             CU(cudaMemcpy(d_tiles[b], tiles[b].data(), tiles[b].size() * sizeof(int4), cudaMemcpyHostToDevice));
             CU(cudaMemcpy(d_twin[b], twin[b].data(), twin[b].size() * sizeof(int2), cudaMemcpyHostToDevice));
         }
@@ -1105,7 +1111,7 @@ struct Engine {
     int set_launch(int blk, int ctas) {
         if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
         const int bi = block_index(blk);
-        if (bi < 0) return fail(VISG_ERR_INVALID_ARG, "block must be 128, 256 or 512");
+        if (bi < 0) return fail(VISG_ERR_INVALID_ARG, "block must be 128, 256, 512 or 1024");
         if (ctas < 0 || (ctas > 0 && ctas > step_max_ctas_per_sm(variant(blk), blk, win_cap[bi])))
             return fail(VISG_ERR_INVALID_ARG, "ctas_per_sm out of range for this block size");
         if (int r = sync()) return r;
@@ -1155,10 +1161,10 @@ struct Engine {
         int best_block = block, best_grid = grid, best_ctas = 0, best_split = split, best_stage = stage;
         const int split0 = split, stage0 = stage;
         const int n_split = (p.collide && any_body) ? 2 : 1;
-        for (int sv = 0; sv < 2 * n_split * 3 && e == cudaSuccess; ++sv) {
-            stage = sv / (3 * n_split);
-            split = (sv / 3) % n_split;
-            const int bi = sv % 3;
+        for (int sv = 0; sv < 2 * n_split * kNumBlocks && e == cudaSuccess; ++sv) {
+            stage = sv / (kNumBlocks * n_split);
+            split = (sv / kNumBlocks) % n_split;
+            const int bi = sv % kNumBlocks;
             const int blk = kBlocks[bi];
             if (stage && win_cap[bi] == 0) continue;
             const int occ = step_max_ctas_per_sm(variant(blk), blk, win_cap[bi]);

@@ -500,7 +500,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return true;
 }
 
-// thread 0: stage the sliced-ELL block of `tile` at shared address dst, completing
+// the stager: stage the sliced-ELL block of `tile` at shared address dst, completing
 // the buffer's `full` phase when it lands; a tile without a staged block completes
 // the phase at once (every tile takes one phase, so no warp runs ahead of the ring)
 __device__ __forceinline__ void stage_entries(const StepArgs& a, int tile, uint32_t dst, uint32_t full) {
@@ -513,16 +513,20 @@ __device__ __forceinline__ void stage_entries(const StepArgs& a, int tile, uint3
     }
 }
 
-// The fused step: persistent CTAs walk the tile table.  With STAGED, thread 0 copies
-// the next tile's block of sliced-ELL entries (the tile's slices are contiguous: one
-// TMA bulk copy) into the other shared-memory buffer while the warps compute the
-// current tile, so each spring's chain starts with a shared-memory load; tiles whose
-// block exceeds the buffer read their entries from global memory.  No CTA barrier
-// per tile: warps report a finished buffer on its `empty` mbarrier and only thread 0
-// waits for it before refilling.  Waits are bounded: one that gives up after kWaitNs
-// sets ERR_TIMEOUT, the issuing thread waits (again bounded) for its copies in
-// flight, and the warp exits; warps left waiting on a copy that is never issued give
-// up the same way.
+// The fused step: persistent CTAs walk the tile table.  With STAGED, one thread (the
+// stager) copies the next tile's block of sliced-ELL entries (the tile's slices are
+// contiguous: one TMA bulk copy) into the other shared-memory buffer while the warps
+// compute the current tile, so each spring's chain starts with a shared-memory load;
+// tiles whose block exceeds the buffer read their entries from global memory.  No CTA
+// barrier per tile: warps report a finished buffer on its `empty` mbarrier and only
+// the stager waits for it before refilling.  The stager of iteration `it` is lane 0 of
+// warp it % (BLOCK / 32), so the wait for the slowest warp and the copy's issue
+// latency fall on each warp once per BLOCK / 32 tiles.  With thread 0 as the only
+// stager they fell on warp 0 every tile, and warp 0 paced the CTA: the other warps
+// ran up to a tile ahead and then waited on `full`.  Waits are bounded: one that
+// gives up after kWaitNs sets ERR_TIMEOUT, the iteration's stager waits (again
+// bounded) for the copies in flight, and the warp exits; warps left waiting on a
+// copy that is never issued give up the same way.
 template <int BLOCK, bool COLL, bool KD0, bool SPLIT, bool STAGED>
 __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv, const int check, const int perk) {
     extern __shared__ __align__(128) unsigned char dyn_smem[];
@@ -555,17 +559,18 @@ __global__ void __launch_bounds__(BLOCK) k_step(const StepArgs a, const int refv
             const int b = it & 1;
             const uint32_t par = (uint32_t)(it >> 1) & 1u;  // phase parity of this iteration's buffer
             const int nxt = tile + (int)gridDim.x;
+            const uint32_t stager = (uint32_t)(it % (BLOCK / 32)) * 32u;
             bool pok = true;
-            if (threadIdx.x == 0 && nxt < a.n_tiles) {
+            if (threadIdx.x == stager && nxt < a.n_tiles) {
                 // the other buffer was read in iteration it - 1: wait for every warp to finish it
                 if (it >= 1) pok = mbar_wait(empty + 8u * (b ^ 1), (uint32_t)((it - 1) >> 1) & 1u);
                 if (pok) stage_entries(a, nxt, buf0 + (uint32_t)(b ^ 1) * bbytes, full + 8u * (b ^ 1));
             }
             const bool landed = mbar_wait(full + 8u * b, par);
             if (!__all_sync(0xffffffffu, landed && pok)) {
-                // a wait gave up: record it; the issuing thread lets its copies in flight land
+                // a wait gave up: record it; the stager lets the copies in flight land
                 if (lane == 0) atomicOr(a.err, ERR_TIMEOUT);
-                if (threadIdx.x == 0) {
+                if (threadIdx.x == stager) {
                     mbar_wait(full + 8u * b, par);
                     if (pok && nxt < a.n_tiles) mbar_wait(full + 8u * (b ^ 1), (uint32_t)((it + 1) >> 1) & 1u);
                 }
@@ -925,6 +930,7 @@ cudaError_t launch_step(const StepArgs& a, int variant, int block, int grid, cud
         case 128: return launch_block<128>(a, variant, grid, s);
         case 256: return launch_block<256>(a, variant, grid, s);
         case 512: return launch_block<512>(a, variant, grid, s);
+        case 1024: return launch_block<1024>(a, variant, grid, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -938,6 +944,7 @@ int step_max_ctas_per_sm(int variant, int block, int win_cap) {
         case 128: return occupancy_block<128>(variant, win_cap);
         case 256: return occupancy_block<256>(variant, win_cap);
         case 512: return occupancy_block<512>(variant, win_cap);
+        case 1024: return occupancy_block<1024>(variant, win_cap);
         default: return 0;
     }
 }
