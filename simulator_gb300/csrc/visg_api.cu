@@ -155,7 +155,6 @@ struct Engine {
     uint32_t* d_check = nullptr;
     int2* d_cand = nullptr;            // split collision: queued candidates
     uint32_t* d_cand_count = nullptr;
-    int* d_hitleaf = nullptr;          // query cache: first-hit leaf per vertex
     // output stage: faces of each garment (local indices), and on the device all
     // garments' faces with global indices, the vertex -> face CSR, the face normals
     std::vector<std::vector<uint32_t>> gfaces;
@@ -443,7 +442,6 @@ struct Engine {
         arena.want(&d_check, 4);
         arena.want(&d_cand, (size_t)N + 1);
         arena.want(&d_cand_count, 4);
-        arena.want(&d_hitleaf, (size_t)N + 1);
         arena.want(&d_stage, 10 * (size_t)N + 4);
         bvh.resize(G);
         for (int g = 0; g < G; ++g)
@@ -563,7 +561,6 @@ struct Engine {
         a.check = d_check;
         a.cand = d_cand + ((two && grp == 1) ? vsplit : 0);  // a group queues at most its own vertices
         a.cand_count = d_cand_count + ((two && grp == 1) ? 1 : 0);
-        a.hitleaf = d_hitleaf;
         a.sell = d_sell;
         a.sellk = d_sellk;
         a.slice_off = d_slice_off;
@@ -1151,7 +1148,7 @@ struct Engine {
                                     cudaMemcpyDeviceToDevice, stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(d_normal, bn, (size_t)N * sizeof(float4), cudaMemcpyDeviceToDevice, stream);
-            // the query caches refer to hitleaf, which the timed steps overwrote
+            // the query caches refer to the timed steps' answers
             if (e == cudaSuccess) e = launch_clear_margin(d_state[cur], 0, N, stream);
         };
         cudaEvent_t e0, e1;

@@ -2,15 +2,16 @@
 //
 // HBM layout (all arrays 16-byte aligned, one allocation per engine):
 //   cloth state, double-buffered: 2 float4 per vertex
-//        [x.x x.y x.z v.x] [v.y v.z flags 0]             32 B, one sector per gather
+//        [x.x x.y x.z v.x] [v.y v.z flags margin]        32 B, one sector per gather
 //        v = (x - x_old) / dt, computed once per step by the vertex's own thread;
 //        with StepParams::drec the record carries D = x - x_old in its place (then
 //        no spring reads a neighbour's velocity and the step needs only x - x_old);
 //        x_old is x (flag XO_IS_X) or the x of the same vertex in the other buffer;
 //        the last word is the query cache's margin: while the vertex stays within
 //        that distance of where its last first-hit query was answered, the answer
-//        (no leaf, or hitleaf[i] when flags has LEAF_CACHED) still holds (0 = none)
-//   hitleaf: i32 per vertex, the cached first-hit leaf
+//        (no leaf, or with flag LEAF_CACHED the leaf in the flags word's bits 3-31)
+//        still holds (0 = none); the leaf travels in the record, so a vertex whose
+//        answer is cached reads no other per-vertex array to find it
 //   contact normal (previous step):  float4 per vertex, read only when flags says so
 //   rowp:   u32 per vertex + 1, merged CSR row offsets; bit 31 = vertex pinned
 //   ent:    uint2 per directed spring {end | list << 30, rest}         8 B
@@ -48,7 +49,9 @@ constexpr uint32_t END_MASK = 0x3fffffffu;
 constexpr int LIST_SHIFT = 30;
 constexpr uint32_t FLAG_HAS_NORMAL = 1u;  // the previous contact normal is stored (non-zero)
 constexpr uint32_t FLAG_XO_IS_X = 2u;     // x_old equals x (else x_old = x of the other buffer)
-constexpr uint32_t FLAG_LEAF_CACHED = 4u; // the query cache's answer is the leaf in hitleaf (else no leaf)
+constexpr uint32_t FLAG_LEAF_CACHED = 4u; // the query cache's answer is the leaf in bits 3-31 (else no leaf)
+constexpr int LEAF_SHIFT = 3;                // the cached leaf's position in the flags word
+constexpr int kLeafCacheMax = 1 << 29;       // leaves from this index on are not cached (they do not fit)
 
 // error bits written by kernels into the engine's error word
 constexpr int ERR_STACK = 1;     // traversal stack would overflow (not reachable for <= 30-bit codes)
@@ -176,7 +179,6 @@ struct StepArgs {
     uint32_t* check;  // [0] max |dx| bits, [1] non-finite count
     int2* cand;       // split collision: {vertex, garment} of the vertices inside their body's box
     uint32_t* cand_count;
-    int* hitleaf;             // query cache: first-hit leaf of each vertex's last query
     const uint2* sell;        // sliced-ELL springs (see the layout above)
     const float* sellk;       // per-entry stiffness in the same layout, with SV_PERK
     const uint32_t* slice_off;
