@@ -399,7 +399,7 @@ struct Engine {
                 for (int64_t v = voff[g]; v < voff[g + 1]; v += kBlocks[b]) {
                     const int64_t v1 = std::min<int64_t>(v + kBlocks[b], voff[g + 1]);
                     const int64_t s0 = slice0[g] + (v - voff[g]) / 32, s1 = s0 + (v1 - v + 31) / 32;
-                    tiles[b].push_back(make_int4(g, (int)v, (int)v1, (int)s0));
+                    tiles[b].push_back(make_int4(g | (gin[g].nt > 0 ? TILE_BODY : 0), (int)v, (int)v1, (int)s0));
                     const int64_t cnt = (int64_t)soff[s1] - soff[s0];
                     if (cnt > 0 && cnt <= cap && soff[s1] <= 0x7fffffffu) {
                         twin[b].push_back(make_int2((int)soff[s0], (int)cnt));
@@ -417,7 +417,7 @@ struct Engine {
             vsplit = voff[gs];
             for (int b = 0; b < kNumBlocks; ++b) {
                 tsplit[b] = 0;
-                while (tsplit[b] < (int)tiles[b].size() && tiles[b][tsplit[b]].x < gs) ++tsplit[b];
+                while (tsplit[b] < (int)tiles[b].size() && (tiles[b][tsplit[b]].x & TILE_GARMENT) < gs) ++tsplit[b];
             }
         }
         // plan the allocation

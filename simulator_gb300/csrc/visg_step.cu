@@ -325,7 +325,8 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
         // the record's flags word (the sector s0 came in): start the loads that a cached
         // contact answer and a stored normal need after the spring sum
         const uint32_t fl0 = __float_as_uint(__ldg(reinterpret_cast<const float*>(a.state_in + 2 * ii + 1) + 2));
-        if (fl0 & FLAG_LEAF_CACHED) prefetch_contact(a.bodies[td.x].leaves + 2 * (fl0 >> LEAF_SHIFT));
+        if (fl0 & FLAG_LEAF_CACHED)
+            prefetch_contact(a.bodies[td.x & TILE_GARMENT].leaves + 2 * (fl0 >> LEAF_SHIFT));
         if (fl0 & FLAG_HAS_NORMAL) prefetch_contact(a.normal + ii);
     }
     f3 xn = x, xon = x, nn = mk3(0.0f, 0.0f, 0.0f);
@@ -394,8 +395,8 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
     float skin = 0.0f;
     uint32_t leaf_bits = 0u;  // the cached leaf, in the flags word's place (0: no leaf cached)
     if (COLL) {
-        const BvhView bv = a.bodies[td.x];
-        const bool body = bv.root != nullptr && bv.root->n_leaves > 0;
+        const int g = td.x & TILE_GARMENT;
+        const bool body = (td.x & TILE_BODY) != 0;  // the garment has a body (its tree has leaves)
         bool query = false;
         int leaf = -1;
         if (body && active && !pinned) {
@@ -419,19 +420,20 @@ __device__ __forceinline__ void vertex_step(const StepArgs& a, const int4 td, co
                 uint32_t base = 0;
                 if (lane == leader) base = atomicAdd(a.cand_count, (uint32_t)__popc(m));
                 base = __shfl_sync(0xffffffffu, base, leader);
-                if (query) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, td.x);
+                if (query) a.cand[base + __popc(m & ((1u << lane) - 1u))] = make_int2(i, g);
             }
         } else if (__any_sync(0xffffffffu, query) && query) {
             float m = __int_as_float(0x7f800000);  // +inf
-            leaf = query_margin(bv, xn, a.err, m);
+            leaf = query_margin(a.bodies[g], xn, a.err, m);
             if (P.margin) {
                 skin = m;
                 if (leaf >= 0 && leaf < kLeafCacheMax) leaf_bits = ((uint32_t)leaf << LEAF_SHIFT) | FLAG_LEAF_CACHED;
             }
         }
         if (leaf >= 0) {  // plane test of the first-hit leaf (primitive.cu:110-125)
-            const float4 L0 = __ldg(&bv.leaves[2 * leaf]);
-            const float4 L1 = __ldg(&bv.leaves[2 * leaf + 1]);
+            const float4* const leaves = a.bodies[g].leaves;
+            const float4 L0 = __ldg(&leaves[2 * leaf]);
+            const float4 L1 = __ldg(&leaves[2 * leaf + 1]);
             const f3 n = mk3(L0.w, L1.x, L1.y);
             const float d = dot(sub(xn, mk3(L0.x, L0.y, L0.z)), n);
             if (!(d > 0.0f)) {
