@@ -488,7 +488,7 @@ def test_full_bench_batch_equals_plain_garments():
     for cloth, body in items:
         b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
     b.finalize()
-    b.set_launch(512, 2)
+    b.set_launch(1024, 1)  # the shape the autotuner picks on this batch
     b.step(2400)
     assert b.count_contacts() > 100_000
     sizes = np.array([len(c.xyz) for c, _ in items])
@@ -585,10 +585,40 @@ def test_batch_autotune_keeps_state_and_results():
     a.step(10)
     c.step(10)
     blk, ctas = a.autotune()
-    assert blk in (128, 256, 512)
+    assert blk in (128, 256, 512, 1024)
     a.step(30)
     c.step(30)
     assert np.array_equal(a.positions(), c.positions())
+
+
+@pytest.mark.parametrize("stage", [0, 1])
+def test_every_launch_shape_steps_alike(stage):
+    """Every tile size (128, 256, 512, 1024 vertices), as persistent CTAs (one per SM)
+    or one CTA per tile, staged or not: the same trajectories bit for bit.  The
+    garments' sizes leave a partial last tile at every tile size, and the sheets
+    reach their spheres, so queued queries and cached contact answers are part of it."""
+    p = scenes.physics_params(4)
+    p.stage_neighbours = stage
+    items = [(scenes.grid_cloth(s, 0.6, 0.0), scenes.icosphere(3, 0.25, (0.0, -0.26, 0.0))) for s in (23, 41, 57)]
+    ref = None
+    for blk in (128, 256, 512, 1024):
+        for ctas in (1, 0):
+            b = vs.BatchSimulator(p)
+            for cloth, body in items:
+                b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+            b.finalize()
+            b.set_launch(blk, ctas)
+            b.step(500)
+            st = [b.state(g) for g in range(len(items))]
+            contacts = b.count_contacts()
+            b.close()
+            if ref is None:
+                ref = st
+                assert contacts > 100
+                continue
+            for u, v in zip(st, ref):
+                for x, y in zip(u, v):
+                    assert np.array_equal(x, y), (blk, ctas)
 
 
 def test_divergence_reported():
