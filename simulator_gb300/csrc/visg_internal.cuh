@@ -53,11 +53,12 @@ constexpr uint32_t FLAG_LEAF_CACHED = 4u; // the query cache's answer is the lea
 constexpr int LEAF_SHIFT = 3;                // the cached leaf's position in the flags word
 constexpr int kLeafCacheMax = 1 << 29;       // leaves from this index on are not cached (they do not fit)
 
-// error bits written by kernels into the engine's error word
 // tile descriptor .x: the garment, and whether it has a body (set at finalize: a body
 // has at least one triangle, so every build of its tree has leaves)
 constexpr int TILE_GARMENT = 0x3fffffff;
 constexpr int TILE_BODY = 0x40000000;
+
+// error bits written by kernels into the engine's error word
 constexpr int ERR_STACK = 1;     // traversal stack would overflow (not reachable for <= 30-bit codes)
 constexpr int ERR_DIVERGED = 2;  // divergence check tripped
 constexpr int ERR_TIMEOUT = 4;   // a bounded look-back wait gave up
