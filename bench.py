@@ -21,7 +21,8 @@ Reported (one JSON line, rank 0):
               landed),
               with the host link's own device-to-host rate for the same bytes
               (its ceiling: every step moves all positions over the link)
-  plain_loop  the same garments as 256 plain simulators stepped one after another
+  plain_loop  the same garments as 256 plain simulators stepped one after another,
+              each autotuned on its own draped state (visg_autotune)
   roofline    the fused step kernel: algorithmic bytes per launch / its launch time
               (CUDA events around each launch, 10 steps as one chain after the timed
               region; the same over the whole step is kept beside it)
@@ -250,7 +251,8 @@ def cpu_baseline(items, params, seconds: float, states=None, settle: int = 0):
 def config0_plain(vs, scenes, torch, params, stream, substeps: int, cpu: bool):
     """The smallest plain workload: a 64 x 64 sheet (1 m, two corners pinned) over an
     icosphere of subdivision 4 (radius 0.3 m) centred 0.5 m below, its stated 200
-    frames (`substeps` steps each) from the initial state.  The GPU runs them as one
+    frames (`substeps` steps each) from the initial state.  The simulator is
+    autotuned first (visg_autotune, state unchanged).  The GPU runs the frames as one
     simulate call (graph replay; CUDA events on the launching stream), then again
     from the same initial state for a second timing; with `cpu`, the oracle (float,
     OpenMP) runs the same steps on the host cores for the CPU row beside it."""
@@ -259,6 +261,7 @@ def config0_plain(vs, scenes, torch, params, stream, substeps: int, cpu: bool):
     sim = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
                        pinned=cloth.pinned)
     sim.set_stream(stream.cuda_stream)
+    sim.autotune()
     zero = np.zeros_like(cloth.xyz)
     sim.simulate(steps)  # warm: graph capture, first launches
     times = []
@@ -276,7 +279,7 @@ def config0_plain(vs, scenes, torch, params, stream, substeps: int, cpu: bool):
            "triangles": int(len(body.tris)), "frames": 200, "steps": steps,
            "gpu": {"value": n * steps / (ms / 1e3), "unit": "vertex-steps/s", "ms_per_step": ms / steps,
                    "how": "one simulate call of all steps (graph replay), best of 2 from the initial state"},
-           "contacts_at_end": sim.count_contacts()}
+           "contacts_at_end": sim.count_contacts(), "launch": sim.launch_info()}
     sim.close()
     if cpu:
         from oracle.ffi import OracleSim, num_threads
@@ -297,7 +300,8 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
     `substeps` steps per frame), from the initial state: the sheet falls, meets the
     moving body and drapes over it.  Per step the body's positions (precomputed on the
     device) go in through update_body_device, then one step runs.  Then `steps` more
-    steps with the body held still show the rebuild's share."""
+    steps with the body held still show the rebuild's share.  Each simulator is
+    autotuned when created (visg_autotune, state unchanged)."""
     out = {}
     for name, make, frames in (("garment_over_capsules", scenes.garment_over_capsules, 1000),
                                ("sheet_over_noisy_sphere", scenes.sheet_over_noisy_sphere, 500)):
@@ -306,6 +310,7 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
         sim = vs.Simulator(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, params=params,
                            pinned=cloth.pinned)
         sim.set_stream(stream.cuda_stream)
+        sim.autotune()
         timed = frames * substeps
         total = warmup + timed
         offs = np.stack([motion(k * params.dt) for k in range(total)]).astype(np.float32)
@@ -338,7 +343,7 @@ def moving_body_configs(vs, scenes, torch, params, stream, steps: int, warmup: i
                      "triangles": int(len(body.tris)), "frames": frames, "steps": timed,
                      "value": n / (ms_move / 1e3), "unit": "vertex-steps/s", "ms_per_step": ms_move,
                      "ms_per_step_body_still": ms_still, "lbvh_rebuild_ms": ms_move - ms_still,
-                     "contacts_at_end": contacts}
+                     "contacts_at_end": contacts, "launch": sim.launch_info()}
         del d_frames
         sim.close()
     return out
@@ -576,6 +581,7 @@ def main():
                              pinned=cloth.pinned)
             s.set_state(*b.state(g))  # the batch's draped state
             s.set_stream(sh)
+            s.autotune()  # each plain simulator at its own best launch shape and variant
             sims.append(s)
         for s in sims:
             s.simulate(args.warmup)
@@ -587,8 +593,11 @@ def main():
         p1.record(stream)
         torch.cuda.synchronize()
         pms = max_over_ranks(p0.elapsed_time(p1))
+        split_n = sum(s.launch_info()["split_collision"] for s in sims)
         plain = {"value": nv_all * args.steps / (pms / 1e3), "ms_per_step": pms / args.steps,
-                 "how": "each garment its own Simulator, stepped K steps (graph replay) one garment after another"}
+                 "how": "each garment its own Simulator, autotuned on its draped state, stepped K steps "
+                        "(graph replay) one garment after another",
+                 "autotuned_split_collision": f"{split_n} of {len(sims)}"}
         for s in sims:
             s.close()
     moving = config0 = None

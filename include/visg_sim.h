@@ -64,10 +64,10 @@ typedef struct VisgParams {
     int32_t use_graph;     /* 1: replay multi-step loops as CUDA graphs (default), 0: launches  */
     int32_t split_collision; /* 1: collision in its own kernel over the vertices inside a body's
                                 box (default), 0: fused into the step kernel; same results.
-                                visg_batch_autotune may change it.                             */
+                                visg_autotune / visg_batch_autotune may change it.             */
     int32_t stage_neighbours; /* 1: each tile's block of spring entries is staged in shared
                                 memory by TMA bulk copies, 0: read through the L1 (default);
-                                same results.  visg_batch_autotune may change it.              */
+                                same results.  visg_autotune / visg_batch_autotune may change it. */
     int32_t collision_margin; /* 1: each vertex caches its last first-hit query's answer with
                                 a margin (how far it may move before any box the query
                                 tested could answer differently) and reuses the answer
@@ -201,6 +201,18 @@ int visg_count_contacts(VisgSim* sim, int64_t* n);
 
 int visg_get_info(VisgSim* sim, int32_t* n_vertices, int32_t* n_entries,
                   int32_t* n_tris, int32_t* n_leaves);
+
+/* Times the candidate launch shapes and variants of the step kernel (tile size,
+ * persistent CTAs per SM, collision split into its own kernel or fused, spring
+ * entries staged or not) on this simulator's own data from its current state, keeps
+ * the fastest and leaves the state unchanged, as visg_batch_autotune does for a
+ * batch; *block and *ctas_per_sm (may be NULL) report the choice.  For one garment
+ * the fused collision usually wins: a step is then one kernel.  No counterpart in the
+ * reference (it launches one fixed shape). */
+int visg_autotune(VisgSim* sim, int32_t* block, int32_t* ctas_per_sm);
+/* The launch shape and variant in use, as visg_batch_launch_info. */
+int visg_launch_info(VisgSim* sim, int32_t* block, int32_t* ctas_per_sm, int32_t* split_collision,
+                     int32_t* stage_neighbours, int32_t* kernels_per_step);
 
 /* Inspection of the current LBVH in the reference's layout (bvh.cu:264-297,
  * cudaBRT.h:34-115).  Arrays are host memory sized for n_tris (per-triangle) or

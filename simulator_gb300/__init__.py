@@ -88,6 +88,8 @@ def lib():
         "visg_batch_set_vertex": (C.c_int, [_vp, C.c_int32, C.c_uint32, _fp]),
         "visg_batch_update_body": (C.c_int, [_vp, C.c_int32, _fp, _fp]),
         "visg_batch_autotune": (C.c_int, [_vp, _i32p, _i32p]),
+        "visg_autotune": (C.c_int, [_vp, _i32p, _i32p]),
+        "visg_launch_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, _i32p]),
         "visg_batch_set_launch": (C.c_int, [_vp, C.c_int32, C.c_int32]),
         "visg_batch_launch_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, _i32p]),
         "visg_batch_read_positions_async": (C.c_int, [_vp, _vp]),
@@ -290,6 +292,19 @@ class Simulator:
         a, b, c, d = (C.c_int32() for _ in range(4))
         _check(lib().visg_get_info(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
         return dict(n_vertices=a.value, n_entries=b.value, n_tris=c.value, n_leaves=d.value)
+
+    def autotune(self):
+        """Time the step kernel's launch shapes and variants on this simulator's data
+        and keep the fastest (the state is unchanged); returns (block, ctas_per_sm)."""
+        b, c = C.c_int32(), C.c_int32()
+        _check(lib().visg_autotune(self.h, C.byref(b), C.byref(c)))
+        return b.value, c.value
+
+    def launch_info(self) -> dict:
+        v = [C.c_int32() for _ in range(5)]
+        _check(lib().visg_launch_info(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("block", "ctas_per_sm", "split_collision", "stage_neighbours", "kernels_per_step"),
+                        (x.value for x in v)))
 
     def export_lbvh(self) -> dict:
         T = self.n_tris

@@ -1629,10 +1629,8 @@ int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas) {
     return b->eng.set_launch(block, ctas);
 }
 
-int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas, int32_t* split, int32_t* stage,
-                           int32_t* kernels) {
-    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
-    const Engine& e = b->eng;
+static int launch_info(const Engine& e, int32_t* block, int32_t* ctas, int32_t* split, int32_t* stage,
+                       int32_t* kernels) {
     const int v = e.variant(e.block);
     if (block) *block = e.block;
     if (ctas) *ctas = e.sm_count > 0 ? e.grid / e.sm_count : 0;
@@ -1640,6 +1638,23 @@ int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas, int32_t*
     if (stage) *stage = (v & SV_STAGED) ? 1 : 0;
     if (kernels) *kernels = ((v & SV_SPLIT) ? 2 : 1) * e.groups();
     return VISG_OK;
+}
+
+int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas, int32_t* split, int32_t* stage,
+                           int32_t* kernels) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return launch_info(b->eng, block, ctas, split, stage, kernels);
+}
+
+int visg_autotune(VisgSim* sim, int32_t* block, int32_t* ctas) {
+    ApiRange range_("visg_autotune");
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return sim->eng.autotune(block, ctas);
+}
+
+int visg_launch_info(VisgSim* sim, int32_t* block, int32_t* ctas, int32_t* split, int32_t* stage, int32_t* kernels) {
+    if (!sim) return fail(VISG_ERR_INVALID_ARG, "sim is NULL");
+    return launch_info(sim->eng, block, ctas, split, stage, kernels);
 }
 
 int visg_batch_info(VisgBatch* b, int32_t* ng, int64_t* nv, int64_t* ne, int64_t* nt) {

@@ -591,6 +591,29 @@ def test_batch_autotune_keeps_state_and_results():
     assert np.array_equal(a.positions(), c.positions())
 
 
+def test_plain_autotune_keeps_state_and_results():
+    """visg_autotune on a single garment (draped over its sphere, so the candidates
+    run with contacts): the state is unchanged and the trajectory after it equals an
+    untuned simulator's, bit for bit."""
+    cloth, cl, body, p = ref_scene(side=40, subdiv=3)
+    a = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    c = vs.Simulator(cloth.xyz, cl, body.xyz, body.tris, body.normals, params=p)
+    a.simulate(120)
+    c.simulate(120)
+    before = a.state()
+    blk, ctas = a.autotune()
+    assert blk in (128, 256, 512, 1024) and ctas >= 0
+    for u, v in zip(before, a.state()):
+        assert np.array_equal(u, v)
+    info = a.launch_info()
+    assert info["block"] == blk and info["kernels_per_step"] == (2 if info["split_collision"] else 1)
+    a.simulate(60)
+    c.simulate(60)
+    for u, v in zip(a.state(), c.state()):
+        assert np.array_equal(u, v)
+    assert a.count_contacts() > 10
+
+
 @pytest.mark.parametrize("stage", [0, 1])
 def test_every_launch_shape_steps_alike(stage):
     """Every tile size (128, 256, 512, 1024 vertices), as persistent CTAs (one per SM)
