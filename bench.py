@@ -649,6 +649,10 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_source,
                          "peak_source": peak_kind,
                          "kernel": "k_step (fused integrate + springs + collision)",
+                         "launch_note": ("launch_ms is the step kernel's own launch over the whole batch on "
+                                         "every SM (one chain); inside the timed two-chain step each launch "
+                                         "covers one garment group on the SMs not left to the other group's "
+                                         "collision pass (config.launch.sms_left_to_collision)"),
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "launch_ms": k_step_ms, "achieved_over_whole_step": achieved_step},
             "kernel_ms": {"k_step": k_step_ms, "k_collide": k_collide_ms,

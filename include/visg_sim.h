@@ -308,6 +308,15 @@ int visg_batch_autotune(VisgBatch* b, int32_t* block, int32_t* ctas_per_sm);
  * 0 for one CTA per tile.  For reproducible timings and for callers that tune
  * offline.  No counterpart in the reference (it launches one fixed shape). */
 int visg_batch_set_launch(VisgBatch* b, int32_t block, int32_t ctas_per_sm);
+/* SMs the step kernel leaves free when the batch steps as two overlapping chains with
+ * persistent CTAs, so that one garment group's collision pass runs beside the other
+ * group's step kernel instead of after it; 0 = none (what visg_batch_set_launch
+ * sets).  visg_batch_autotune chooses it by timing whole steps.  Same results.  No
+ * counterpart in the reference. */
+int visg_batch_set_reserve(VisgBatch* b, int32_t sms);
+/* The SMs left free in the step as it runs now (0 when the launch shape or the single
+ * chain makes the reserve inapplicable). */
+int visg_batch_get_reserve(VisgBatch* b, int32_t* sms);
 /* The launch shape and variant in use (any pointer may be NULL): block, ctas_per_sm
  * (0 = one CTA per tile), split_collision and stage_neighbours as chosen (by the
  * parameters or visg_batch_autotune), and the kernels one step launches. */

@@ -89,6 +89,8 @@ def lib():
         "visg_batch_update_body": (C.c_int, [_vp, C.c_int32, _fp, _fp]),
         "visg_batch_autotune": (C.c_int, [_vp, _i32p, _i32p]),
         "visg_autotune": (C.c_int, [_vp, _i32p, _i32p]),
+        "visg_batch_set_reserve": (C.c_int, [_vp, C.c_int32]),
+        "visg_batch_get_reserve": (C.c_int, [_vp, _i32p]),
         "visg_launch_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, _i32p]),
         "visg_batch_set_launch": (C.c_int, [_vp, C.c_int32, C.c_int32]),
         "visg_batch_launch_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, _i32p]),
@@ -461,11 +463,19 @@ class BatchSimulator:
     def launch_info(self) -> dict:
         v = [C.c_int32() for _ in range(5)]
         _check(lib().visg_batch_launch_info(self.h, *[C.byref(x) for x in v]))
-        return dict(zip(("block", "ctas_per_sm", "split_collision", "stage_neighbours", "kernels_per_step"),
-                        (x.value for x in v)))
+        d = dict(zip(("block", "ctas_per_sm", "split_collision", "stage_neighbours", "kernels_per_step"),
+                     (x.value for x in v)))
+        r = C.c_int32()
+        _check(lib().visg_batch_get_reserve(self.h, C.byref(r)))
+        d["sms_left_to_collision"] = r.value
+        return d
 
     def set_launch(self, block: int, ctas_per_sm: int):
         _check(lib().visg_batch_set_launch(self.h, block, ctas_per_sm))
+
+    def set_reserve(self, sms: int):
+        """SMs the step kernel leaves to the other garment group's collision pass."""
+        _check(lib().visg_batch_set_reserve(self.h, sms))
 
     def info(self):
         g = C.c_int32()

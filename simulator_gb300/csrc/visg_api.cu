@@ -169,6 +169,10 @@ struct Engine {
     uint32_t* h_status = nullptr;  // pinned: err, check0, check1
     int cur = 0;
     int block = 256, grid = 0;
+    // SMs the persistent step kernel leaves free when two garment groups step as
+    // overlapping chains: one group's collision pass then runs beside the other
+    // group's step kernel instead of after it (chosen by the autotuner)
+    int reserve = 0;
     int64_t steps_since_check = 0;
     cudaGraphExec_t chunk_exec[2] = {nullptr, nullptr};
     int chunk_steps = 16;
@@ -572,14 +576,21 @@ struct Engine {
         return a;
     }
 
+    // the step kernel's grid: with two overlapping chains and persistent CTAs, `reserve`
+    // SMs' worth of CTAs fewer
+    int step_grid() const {
+        if (groups() != 2 || grid <= 0 || reserve <= 0 || sm_count <= reserve) return grid;
+        return (grid / sm_count) * (sm_count - reserve);
+    }
+
     // one step; with two groups the second runs on its own stream (forked from and
     // joined back to s) so the two chains overlap as they do in the step graphs
     cudaError_t launch_one(cudaStream_t s, int from) {
         if (groups() == 1) return launch_step(args(from, block, 0), variant(block), block, grid, s);
         cudaError_t e = cudaEventRecord(fork2, s);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(run2, fork2, 0);
-        if (e == cudaSuccess) e = launch_step(args(from, block, 1), variant(block), block, grid, run2);
-        cudaError_t e0 = launch_step(args(from, block, 0), variant(block), block, grid, s);
+        if (e == cudaSuccess) e = launch_step(args(from, block, 1), variant(block), block, step_grid(), run2);
+        cudaError_t e0 = launch_step(args(from, block, 0), variant(block), block, step_grid(), s);
         cudaError_t ej = cudaEventRecord(join2, run2);
         if (ej == cudaSuccess) ej = cudaStreamWaitEvent(s, join2, 0);
         return e != cudaSuccess ? e : (e0 != cudaSuccess ? e0 : ej);
@@ -600,7 +611,7 @@ struct Engine {
         int from = c;
         for (int k = 0; k < chunk_steps && le == cudaSuccess; ++k) {
             for (int gr = 0; gr < ng; ++gr) {
-                cudaError_t e = launch_step(args(from, block, gr), variant(block), block, grid, gr ? cap2 : cap);
+                cudaError_t e = launch_step(args(from, block, gr), variant(block), block, step_grid(), gr ? cap2 : cap);
                 if (e != cudaSuccess && le == cudaSuccess) le = e;
             }
             from ^= 1;
@@ -1112,9 +1123,21 @@ struct Engine {
         if (ctas < 0 || (ctas > 0 && ctas > step_max_ctas_per_sm(variant(blk), blk, win_cap[bi])))
             return fail(VISG_ERR_INVALID_ARG, "ctas_per_sm out of range for this block size");
         if (int r = sync()) return r;
-        if (blk != block || ctas * sm_count != grid) {
+        if (blk != block || ctas * sm_count != grid || reserve != 0) {
             block = blk;
             grid = ctas * sm_count;
+            reserve = 0;
+            destroy_graphs();
+        }
+        return VISG_OK;
+    }
+
+    int set_reserve(int sms) {
+        if (!finalized) return fail(VISG_ERR_STATE, "not finalized");
+        if (sms < 0 || sms >= sm_count) return fail(VISG_ERR_INVALID_ARG, "reserve out of range");
+        if (int r = sync()) return r;
+        if (sms != reserve) {
+            reserve = sms;
             destroy_graphs();
         }
         return VISG_OK;
@@ -1199,18 +1222,48 @@ struct Engine {
         stage = stage0;
         restore();
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e == cudaSuccess &&
+            (best_block != block || best_grid != grid || best_split != split || best_stage != stage || reserve != 0)) {
+            block = best_block;
+            grid = best_grid;
+            split = best_split;
+            stage = best_stage;
+            reserve = 0;
+            destroy_graphs();
+        }
+        // with two overlapping chains of persistent kernels and the collision split out,
+        // time whole steps, replayed from the step graphs as they run (the chains
+        // overlap only there), with SMs left free for the other group's collision pass
+        if (e == cudaSuccess && groups() == 2 && grid > 0 && (variant(block) & SV_SPLIT) && p.use_graph) {
+            float best_r = 1e30f;
+            int best_res = 0;
+            for (int res : {0, 8, 16, 24, 32}) {
+                if (res >= sm_count / 2 || e != cudaSuccess) break;
+                reserve = res;
+                destroy_graphs();
+                restore();
+                if (step(chunk_steps) != VISG_OK) e = cudaErrorUnknown;  // captures this shape's graph
+                if (e == cudaSuccess) e = cudaEventRecord(e0, stream);
+                if (e == cudaSuccess && step(2 * chunk_steps) != VISG_OK) e = cudaErrorUnknown;
+                if (e == cudaSuccess) e = cudaEventRecord(e1, stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (e == cudaSuccess && ms < best_r) {
+                    best_r = ms;
+                    best_res = res;
+                }
+            }
+            reserve = best_res;
+            restore();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            destroy_graphs();
+        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         cudaFree(bs);
         cudaFree(bn);
         if (e != cudaSuccess) return cuda_fail(e, "autotune");
-        if (best_block != block || best_grid != grid || best_split != split || best_stage != stage) {
-            block = best_block;
-            grid = best_grid;
-            split = best_split;
-            stage = best_stage;
-            destroy_graphs();
-        }
         if (out_block) *out_block = block;
         if (out_ctas) *out_ctas = best_ctas;
         return sync();
@@ -1644,6 +1697,17 @@ int visg_batch_launch_info(VisgBatch* b, int32_t* block, int32_t* ctas, int32_t*
                            int32_t* kernels) {
     if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
     return launch_info(b->eng, block, ctas, split, stage, kernels);
+}
+
+int visg_batch_set_reserve(VisgBatch* b, int32_t sms) {
+    if (!b) return fail(VISG_ERR_INVALID_ARG, "batch is NULL");
+    return b->eng.set_reserve(sms);
+}
+
+int visg_batch_get_reserve(VisgBatch* b, int32_t* sms) {
+    if (!b || !sms) return fail(VISG_ERR_INVALID_ARG, "batch or sms is NULL");
+    *sms = b->eng.step_grid() != b->eng.grid ? b->eng.reserve : 0;
+    return VISG_OK;
 }
 
 int visg_autotune(VisgSim* sim, int32_t* block, int32_t* ctas) {

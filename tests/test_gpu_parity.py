@@ -591,6 +591,32 @@ def test_batch_autotune_keeps_state_and_results():
     assert np.array_equal(a.positions(), c.positions())
 
 
+def test_batch_sms_left_to_collision_step_alike():
+    """Leaving SMs free for the other garment group's collision pass (two overlapping
+    chains, persistent step kernels on fewer SMs) changes no result, bit for bit."""
+    p = scenes.physics_params(4)
+    p.stage_neighbours = 1
+    # about 330 tiles of 128 vertices: more than the persistent CTAs, so the grids differ
+    items = [(scenes.grid_cloth(s, 0.6, 0.0), scenes.icosphere(3, 0.25, (0.0, -0.26, 0.0))) for s in (90, 100, 110, 120)]
+    states = []
+    for res in (0, 16, 40):
+        b = vs.BatchSimulator(p)
+        for cloth, body in items:
+            b.add(cloth.xyz, cloth.lists, body.xyz, body.tris, body.normals, pinned=cloth.pinned)
+        b.finalize()
+        b.set_launch(128, 1)
+        b.set_reserve(res)
+        assert b.launch_info()["sms_left_to_collision"] == res
+        b.step(500)
+        assert b.count_contacts() > 100
+        states.append([b.state(g) for g in range(len(items))])
+        b.close()
+    for st in states[1:]:
+        for u, v in zip(st, states[0]):
+            for x, y in zip(u, v):
+                assert np.array_equal(x, y)
+
+
 def test_plain_autotune_keeps_state_and_results():
     """visg_autotune on a single garment (draped over its sphere, so the candidates
     run with contacts): the state is unchanged and the trajectory after it equals an
